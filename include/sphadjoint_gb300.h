@@ -1,0 +1,169 @@
+/*
+ * sphadjoint_gb300 — C ABI of the GB300 (sm_103a) forward + adjoint WCSPH step.
+ *
+ * A drop-in for the device path of the Julia package SPHAdjoint
+ * (hanafsky/SPHAdjoint): each entry point below replaces one public function
+ * or constructor of that package, cited as file:line in its source tree. The
+ * Julia side binds them with `ccall` (a thin wrapper keeps the names
+ * SPHParams / State / Tape / AdjointWorkspace / simulate! / backward!).
+ *
+ * Conventions (the reference's own):
+ *   - T is Float64 (SPH_F64) or Float32 (SPH_F32), fixed per object.
+ *   - Host arrays X, V, seeds, gradients: (2, N) column-major T, i.e.
+ *     interleaved (x1, y1, x2, y2, ...). theta and dJ/dtheta: (ngy, ngx)
+ *     column-major T.
+ *   - Cell lists use 1-based particle ids in `order` and 0-based exclusive
+ *     offsets in `starts`, exactly as CellList holds them.
+ *   - Every call returns a status (SPH_OK = 0); on failure sph_last_error()
+ *     gives the message. No exception crosses the ABI. There is no CPU
+ *     fallback: without a CUDA device every device call fails loudly.
+ *   - One library stream; a handle is used by one host thread at a time.
+ */
+#ifndef SPHADJOINT_GB300_H
+#define SPHADJOINT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_API __attribute__((visibility("default")))
+
+/* SPHParams{T} (src/params.jl:58-72). gx/gy default to 0 / -9.81 there. */
+typedef struct sph_params {
+    double h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
+    int32_t ngx, ngy;
+} sph_params;
+
+typedef struct sph_state_s *sph_state;         /* State          (src/driver.jl:5-36)   */
+typedef struct sph_tape_s *sph_tape;           /* Tape           (src/driver.jl:45-65)  */
+typedef struct sph_workspace_s *sph_workspace; /* AdjointWorkspace (src/driver.jl:117-133) */
+typedef struct sph_field_s *sph_field;         /* device theta   (the `theta` argument)  */
+
+enum { SPH_F64 = 0, SPH_F32 = 1 };
+
+enum {
+    SPH_OK = 0,
+    SPH_ERR_ARG = 1,      /* ArgumentError in the reference */
+    SPH_ERR_CAPACITY = 2, /* tape capacity exceeded (simulate!, src/driver.jl:94-99) */
+    SPH_ERR_CUDA = 3,
+    SPH_ERR_DTYPE = 4,
+    SPH_ERR_NOMEM = 5,
+    SPH_ERR_STATE = 6
+};
+
+/* neighbour-list flags read (and cleared) at the API boundary
+   (check_neighbor_flags, src/neighbors.jl:282-290) */
+enum {
+    SPH_FLAG_NL_OVERFLOW = 1,  /* flags[1]: a row exceeded maxnb */
+    SPH_FLAG_DISPLACEMENT = 2, /* flags[2]: displacement > skin*h before a rebuild */
+    SPH_FLAG_NONFINITE = 4     /* non-finite position/velocity produced (no reference flag) */
+};
+
+SPH_API const char *sph_last_error(void);
+SPH_API int32_t sph_version(void);
+/* Use an external CUDA stream (cudaStream_t) instead of the library's own. */
+SPH_API int32_t sph_set_stream(void *cuda_stream);
+SPH_API int32_t sph_synchronize(void);
+
+/* ---- design field theta: KernelAbstractions.allocate + copyto!(th, theta) ---- */
+SPH_API int32_t sph_field_create(int32_t ngx, int32_t ngy, int32_t dtype, const void *theta,
+                                 sph_field *out);
+SPH_API int32_t sph_field_upload(sph_field th, const void *theta);
+/* theta already on the device (e.g. a CuArray): device-to-device copy */
+SPH_API int32_t sph_field_upload_device(sph_field th, const void *theta_dev);
+SPH_API int32_t sph_field_destroy(sph_field th);
+
+/* ---- State(backend, X0, V0, p; skin, interval, maxnb) (src/driver.jl:24-36) ---- */
+SPH_API int32_t sph_state_create(const sph_params *p, int64_t N, const void *X0, const void *V0,
+                                 int32_t dtype, double skin, int32_t interval, int32_t maxnb,
+                                 sph_state *out);
+SPH_API int32_t sph_state_destroy(sph_state st);
+/* copyto!(st.X, X) / copyto!(st.V, V); either may be NULL */
+SPH_API int32_t sph_state_set(sph_state st, const void *X, const void *V);
+/* Array(st.X), Array(st.V) */
+SPH_API int32_t sph_state_get(sph_state st, void *X, void *V);
+/* Array(st.rho), st.pterm, st.invrho, st.a, st.alpha (a/alpha need keep_accel) */
+SPH_API int32_t sph_state_fields(sph_state st, void *rho, void *pterm, void *invrho, void *a,
+                                 void *alpha);
+/* keep st.a and st.alpha up to date on every step (off by default: the fused
+   accel+integrate kernel does not need them) */
+SPH_API int32_t sph_state_keep_accel(sph_state st, int32_t on);
+/* check_neighbor_flags (src/neighbors.jl:282-290): read and clear */
+SPH_API int32_t sph_state_take_flags(sph_state st, uint32_t *flags);
+SPH_API int32_t sph_state_grid(sph_state st, int32_t *nx, int32_t *ny, double *cs, int64_t *age);
+
+/* build!(cl, X, p, backend) (src/neighbors.jl:97-114) */
+SPH_API int32_t sph_build_cells(sph_state st);
+/* build_neighbors!(nl, cl, X, p, backend) (src/neighbors.jl:252-263) */
+SPH_API int32_t sph_build_neighbors(sph_state st);
+/* CellList counts (ncell), starts (ncell, 0-based), order (N, 1-based ids) */
+SPH_API int32_t sph_get_celllist(sph_state st, int32_t *counts, int32_t *starts, int32_t *order);
+/* NeighborList rows, particle-major: indices[(i-1)*maxnb + m] (1-based ids) */
+SPH_API int32_t sph_get_neighbors(sph_state st, int32_t *indices, int32_t *nbcount);
+
+/* step!(st, theta, p, backend) (src/forward.jl:161-173); p may be NULL (use the
+   state's parameters). Does not synchronise. */
+SPH_API int32_t sph_step(sph_state st, sph_field theta, const sph_params *p);
+/* simulate!(st, theta, p, backend, nsteps; tape) (src/driver.jl:92-115); tape
+   may be NULL; *flags (may be NULL) receives the neighbour-list flags. */
+SPH_API int32_t sph_simulate(sph_state st, sph_field theta, const sph_params *p, int64_t nsteps,
+                             sph_tape tape, uint32_t *flags);
+
+/* ---- Tape(backend, N, nsteps, p) (src/driver.jl:62-65): full (X, V) history ---- */
+SPH_API int32_t sph_tape_create(int64_t N, int64_t nsteps, int32_t dtype, sph_tape *out);
+/* Binomial checkpoint tape: keeps `nsnapshots` device snapshots (each holding the
+   full state and its neighbour structure) and recomputes the forward during
+   backward (no counterpart in the reference, which stores every step;
+   src/driver.jl:56-60 names it as the next step). */
+SPH_API int32_t sph_tape_create_checkpointed(int64_t N, int64_t nsteps, int32_t nsnapshots,
+                                             int32_t dtype, sph_tape *out);
+SPH_API int32_t sph_tape_destroy(sph_tape tp);
+/* reset!(tape) (src/driver.jl:71) */
+SPH_API int32_t sph_tape_reset(sph_tape tp);
+/* length(tape) (src/driver.jl:67) */
+SPH_API int32_t sph_tape_length(sph_tape tp, int64_t *n);
+/* tape.X[:, :, n], tape.V[:, :, n] (1-based n; full tapes only) */
+SPH_API int32_t sph_tape_get(sph_tape tp, int64_t n, void *X, void *V);
+/* forward steps recomputed by the last backward over this tape */
+SPH_API int32_t sph_tape_recomputed_steps(sph_tape tp, int64_t *n);
+
+/* ---- AdjointWorkspace(backend, N, p) (src/driver.jl:128-133) ---- */
+SPH_API int32_t sph_workspace_create(int64_t N, const sph_params *p, int32_t dtype,
+                                     sph_workspace *out);
+SPH_API int32_t sph_workspace_destroy(sph_workspace ws);
+/* backward!(ws, tape, theta, p, backend; seedX, seedV, scratch, skin, interval,
+   maxnb) (src/driver.jl:141-207). seeds are host arrays (NULL = zero); scratch
+   may be NULL (a fresh one, as in the reference). */
+SPH_API int32_t sph_backward(sph_workspace ws, sph_tape tp, sph_field theta,
+                             const sph_params *p, const void *seedX, const void *seedV,
+                             sph_state scratch, double skin, int32_t interval, int32_t maxnb,
+                             uint32_t *flags);
+/* Array(ws.gX), Array(ws.gV), Array(ws.gtheta); any may be NULL */
+SPH_API int32_t sph_workspace_get(sph_workspace ws, void *gX, void *gV, void *gtheta);
+
+/* ---- instrumentation ---- */
+/* kernels launched by this library since load */
+SPH_API int64_t sph_launch_count(void);
+/* time every launch of one kernel id with CUDA events on the library stream */
+SPH_API int32_t sph_profile_enable(int32_t kernel_id, int32_t on);
+SPH_API int32_t sph_profile_read(int32_t kernel_id, double *total_ms, int64_t *launches);
+SPH_API int32_t sph_profile_reset(void);
+/* kernel ids for sph_profile_* */
+enum {
+    SPH_K_ASSIGN = 0, SPH_K_SCAN, SPH_K_BUCKET, SPH_K_RANK, SPH_K_NLBUILD, SPH_K_DENSITY,
+    SPH_K_ACCEL_INTEGRATE, SPH_K_TAPE, SPH_K_GATHER, SPH_K_ACCEL_DRAG, SPH_K_PASS1,
+    SPH_K_PASS2, SPH_K_THETA_NODE, SPH_K_MISC
+};
+
+/* binomial checkpoint schedule (host only): forward steps to reverse l steps
+   with c snapshot slots, and the optimal first split */
+SPH_API int64_t sph_plan_cost(int64_t l, int64_t c);
+SPH_API int64_t sph_plan_split(int64_t l, int64_t c);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

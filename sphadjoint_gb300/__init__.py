@@ -1,0 +1,24 @@
+"""sphadjoint_gb300: the forward + hand-written-adjoint WCSPH step of SPHAdjoint
+(hanafsky/SPHAdjoint), rebuilt as sm_103a CUDA kernels behind a C ABI
+(include/sphadjoint_gb300.h). This package is the Python mirror of the
+reference's Julia API over that ABI."""
+from .api import (  # noqa: F401
+    AdjointWorkspace,
+    DesignField,
+    SPHParams,
+    State,
+    Tape,
+    backward,
+    build,
+    build_neighbors,
+    kinetic_energy_right_half,
+    launch_count,
+    reset,
+    simulate,
+    step,
+    synchronize,
+    target_objective,
+)
+from ._lib import SPHError, CapacityError, ArgumentError, load  # noqa: F401
+
+__version__ = "0.1.0"

@@ -1,0 +1,374 @@
+"""Python mirror of SPHAdjoint's public API over the C ABI.
+
+Names follow the reference module's exports (src/SPHAdjoint.jl:212-213):
+``SPHParams, State, Tape, AdjointWorkspace, simulate, step, build,
+build_neighbors, backward, target_objective, reset`` (Julia's ``simulate!``
+is ``simulate`` here, etc.). Arrays use the reference's shapes: positions,
+velocities, seeds and gradients are (2, N); theta is (ngy, ngx). All compute
+runs in the CUDA library; nothing here falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import warnings
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib as L
+
+_DT = {"f64": (L.SPH_F64, np.float64), "f32": (L.SPH_F32, np.float32)}
+
+
+@dataclass
+class SPHParams:
+    """SPHParams{T} (src/params.jl:58-72); ``dtype`` is T ("f64" or "f32")."""
+
+    h: float
+    m: float
+    rho0: float
+    c: float
+    mu: float
+    dt: float
+    Lx: float
+    Ly: float
+    kw: float
+    ngx: int
+    ngy: int
+    gx: float = 0.0
+    gy: float = -9.81
+    dtype: str = "f64"
+
+    def c_struct(self) -> L.sph_params:
+        p = L.sph_params()
+        for k in ("h", "m", "rho0", "c", "mu", "gx", "gy", "dt", "Lx", "Ly", "kw"):
+            setattr(p, k, float(getattr(self, k)))
+        p.ngx, p.ngy = int(self.ngx), int(self.ngy)
+        return p
+
+    @property
+    def code(self) -> int:
+        return _DT[self.dtype][0]
+
+    @property
+    def np(self):
+        return _DT[self.dtype][1]
+
+    # src/params.jl:74-76
+    def support(self) -> float:
+        return 2 * self.h
+
+    def dxg(self) -> float:
+        return self.Lx / (self.ngx - 1)
+
+    def dyg(self) -> float:
+        return self.Ly / (self.ngy - 1)
+
+
+def _xy(a, N, dt):
+    """(2, N) or (N, 2) -> contiguous (N, 2) of T (the interleaved layout)."""
+    a = np.asarray(a)
+    if a.shape == (2, N):
+        a = a.T
+    return np.ascontiguousarray(a.reshape(N, 2), dtype=dt)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class DesignField:
+    """Device copy of the design field theta, (ngy, ngx) column-major T."""
+
+    def __init__(self, theta, dtype: str = "f64"):
+        self._L = L.load()
+        code, npdt = _DT[dtype]
+        th = np.asarray(theta, dtype=np.float64)
+        self.shape = th.shape
+        self.dtype = dtype
+        ngy, ngx = th.shape
+        h = C.c_void_p()
+        cm = np.asfortranarray(th.astype(npdt))
+        L.check(self._L.sph_field_create(ngx, ngy, code, _ptr(cm), C.byref(h)))
+        self.h = h
+
+    def upload(self, theta):
+        cm = np.asfortranarray(np.asarray(theta, dtype=_DT[self.dtype][1]))
+        if cm.shape != self.shape:
+            raise ValueError("theta shape changed")
+        L.check(self._L.sph_field_upload(self.h, _ptr(cm)))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_field_destroy(self.h)
+            self.h = None
+
+
+def _field(theta, p: SPHParams) -> DesignField:
+    if isinstance(theta, DesignField):
+        return theta
+    return DesignField(theta, p.dtype)
+
+
+class State:
+    """State(backend, X0, V0, p; skin, interval, maxnb) (src/driver.jl:24-36)."""
+
+    def __init__(self, X0, V0, p: SPHParams, skin=0.2, interval=4, maxnb=64):
+        self._L = L.load()
+        self.p = p
+        self.N = N = int(np.asarray(X0).size // 2)
+        self.maxnb = int(maxnb)
+        self.skin, self.interval = float(skin), int(interval)
+        x = _xy(X0, N, p.np)
+        v = _xy(V0, N, p.np)
+        h = C.c_void_p()
+        L.check(self._L.sph_state_create(C.byref(p.c_struct()), N, _ptr(x), _ptr(v), p.code,
+                                         float(skin), int(interval), int(maxnb), C.byref(h)))
+        self.h = h
+        self.last_flags = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_state_destroy(self.h)
+            self.h = None
+
+    # Array(st.X) / Array(st.V): (2, N)
+    def get(self):
+        X = np.empty((self.N, 2), self.p.np)
+        V = np.empty((self.N, 2), self.p.np)
+        L.check(self._L.sph_state_get(self.h, _ptr(X), _ptr(V)))
+        return X.T, V.T
+
+    @property
+    def X(self):
+        return self.get()[0]
+
+    @property
+    def V(self):
+        return self.get()[1]
+
+    def set(self, X=None, V=None):
+        x = _xy(X, self.N, self.p.np) if X is not None else None
+        v = _xy(V, self.N, self.p.np) if V is not None else None
+        L.check(self._L.sph_state_set(self.h, _ptr(x), _ptr(v)))
+
+    def keep_accel(self, on=True):
+        L.check(self._L.sph_state_keep_accel(self.h, int(bool(on))))
+
+    def fields(self, accel=False):
+        N, dt = self.N, self.p.np
+        rho, pt, ir = (np.empty(N, dt) for _ in range(3))
+        a = np.empty((N, 2), dt) if accel else None
+        al = np.empty(N, dt) if accel else None
+        L.check(self._L.sph_state_fields(self.h, _ptr(rho), _ptr(pt), _ptr(ir), _ptr(a), _ptr(al)))
+        out = dict(rho=rho, pterm=pt, invrho=ir)
+        if accel:
+            out.update(a=a.T, alpha=al)
+        return out
+
+    def grid(self):
+        nx, ny, cs, age = C.c_int32(), C.c_int32(), C.c_double(), C.c_int64()
+        L.check(self._L.sph_state_grid(self.h, C.byref(nx), C.byref(ny), C.byref(cs), C.byref(age)))
+        return nx.value, ny.value, cs.value, age.value
+
+    def celllist(self):
+        """CellList counts, starts (0-based), order (1-based ids)."""
+        nx, ny, _, _ = self.grid()
+        counts = np.empty(nx * ny, np.int32)
+        starts = np.empty(nx * ny, np.int32)
+        order = np.empty(max(self.N, 1), np.int32)[: self.N]
+        L.check(self._L.sph_get_celllist(self.h, _ptr(counts), _ptr(starts), _ptr(order)))
+        return dict(counts=counts, starts=starts, order=order)
+
+    def neighbors(self):
+        """NeighborList rows (particle-major, 1-based ids) and counts."""
+        idx = np.zeros((self.N, self.maxnb), np.int32)
+        nbc = np.zeros(self.N, np.int32)
+        L.check(self._L.sph_get_neighbors(self.h, _ptr(idx), _ptr(nbc)))
+        return idx, nbc
+
+    def take_flags(self) -> int:
+        f = C.c_uint32()
+        L.check(self._L.sph_state_take_flags(self.h, C.byref(f)))
+        return f.value
+
+
+def _warn_flags(f: int, maxnb: int):
+    # check_neighbor_flags (src/neighbors.jl:282-290)
+    if f & L.FLAG_NL_OVERFLOW:
+        warnings.warn(f"neighbour-list row overflowed (maxnb={maxnb}); neighbours are missing. "
+                      "Increase maxnb.", RuntimeWarning, stacklevel=3)
+    if f & L.FLAG_DISPLACEMENT:
+        warnings.warn("neighbour-list rebuild interval too long (displacement exceeded skin*h); "
+                      "neighbours may be missing. Lower interval or raise skin.",
+                      RuntimeWarning, stacklevel=3)
+    if f & L.FLAG_NONFINITE:
+        warnings.warn("non-finite positions or velocities were produced", RuntimeWarning,
+                      stacklevel=3)
+
+
+class Tape:
+    """Tape(backend, N, nsteps, p) (src/driver.jl:62-65).
+
+    ``snapshots=0`` keeps every step's (X, V) like the reference. ``snapshots=c``
+    keeps c device snapshots and recomputes the rest during ``backward``
+    (binomial checkpointing), for horizons whose full history would not fit.
+    """
+
+    def __init__(self, N: int, nsteps: int, p: SPHParams, snapshots: int = 0):
+        self._L = L.load()
+        self.N, self.cap, self.p, self.snapshots = int(N), int(nsteps), p, int(snapshots)
+        h = C.c_void_p()
+        if snapshots:
+            L.check(self._L.sph_tape_create_checkpointed(self.N, self.cap, int(snapshots), p.code,
+                                                         C.byref(h)))
+        else:
+            L.check(self._L.sph_tape_create(self.N, self.cap, p.code, C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_tape_destroy(self.h)
+            self.h = None
+
+    def __len__(self):
+        n = C.c_int64()
+        L.check(self._L.sph_tape_length(self.h, C.byref(n)))
+        return n.value
+
+    def capacity(self):
+        return self.cap
+
+    def reset(self):
+        L.check(self._L.sph_tape_reset(self.h))
+        return self
+
+    def get(self, n):
+        X = np.empty((self.N, 2), self.p.np)
+        V = np.empty((self.N, 2), self.p.np)
+        L.check(self._L.sph_tape_get(self.h, int(n), _ptr(X), _ptr(V)))
+        return X.T, V.T
+
+    def recomputed_steps(self):
+        n = C.c_int64()
+        L.check(self._L.sph_tape_recomputed_steps(self.h, C.byref(n)))
+        return n.value
+
+
+class AdjointWorkspace:
+    """AdjointWorkspace(backend, N, p) (src/driver.jl:128-133)."""
+
+    def __init__(self, N: int, p: SPHParams):
+        self._L = L.load()
+        self.N, self.p = int(N), p
+        h = C.c_void_p()
+        L.check(self._L.sph_workspace_create(self.N, C.byref(p.c_struct()), p.code, C.byref(h)))
+        self.h = h
+        self.last_flags = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_workspace_destroy(self.h)
+            self.h = None
+
+    def get(self):
+        gX = np.empty((self.N, 2), self.p.np)
+        gV = np.empty((self.N, 2), self.p.np)
+        gt = np.empty((self.p.ngx, self.p.ngy), self.p.np)  # column-major (ngy, ngx)
+        L.check(self._L.sph_workspace_get(self.h, _ptr(gX), _ptr(gV), _ptr(gt)))
+        return gX.T, gV.T, gt.T
+
+    @property
+    def gX(self):
+        return self.get()[0]
+
+    @property
+    def gV(self):
+        return self.get()[1]
+
+    @property
+    def gtheta(self):
+        return self.get()[2]
+
+
+def reset(tape: Tape) -> Tape:
+    """reset!(tape) (src/driver.jl:71)."""
+    return tape.reset()
+
+
+def build(st: State) -> State:
+    """build!(cl, X, p, backend) (src/neighbors.jl:97-114)."""
+    L.check(st._L.sph_build_cells(st.h))
+    return st
+
+
+def build_neighbors(st: State) -> State:
+    """build_neighbors!(nl, cl, X, p, backend) (src/neighbors.jl:252-263)."""
+    L.check(st._L.sph_build_neighbors(st.h))
+    return st
+
+
+def step(st: State, theta, p: SPHParams | None = None) -> State:
+    """step!(st, theta, p, backend) (src/forward.jl:161-173)."""
+    th = _field(theta, st.p)
+    L.check(st._L.sph_step(st.h, th.h, C.byref(p.c_struct()) if p is not None else None))
+    return st
+
+
+def simulate(st: State, theta, p: SPHParams | None, nsteps: int, tape: Tape | None = None) -> State:
+    """simulate!(st, theta, p, backend, nsteps; tape) (src/driver.jl:92-115)."""
+    th = _field(theta, st.p)
+    f = C.c_uint32()
+    L.check(st._L.sph_simulate(st.h, th.h, C.byref(p.c_struct()) if p is not None else None,
+                               int(nsteps), tape.h if tape is not None else None, C.byref(f)))
+    st.last_flags = f.value
+    _warn_flags(f.value, st.maxnb)
+    return st
+
+
+def backward(ws: AdjointWorkspace, tape: Tape, theta, p: SPHParams, seedX, seedV=None,
+             scratch: State | None = None, skin=0.2, interval=4, maxnb=64) -> AdjointWorkspace:
+    """backward!(ws, tape, theta, p, backend; seedX, seedV, scratch, skin,
+    interval, maxnb) (src/driver.jl:141-207)."""
+    th = _field(theta, p)
+    N = ws.N
+    sx = _xy(seedX, N, p.np) if seedX is not None else None
+    sv = _xy(seedV, N, p.np) if seedV is not None else None
+    f = C.c_uint32()
+    L.check(ws._L.sph_backward(ws.h, tape.h, th.h, C.byref(p.c_struct()), _ptr(sx), _ptr(sv),
+                               scratch.h if scratch is not None else None, float(skin),
+                               int(interval), int(maxnb), C.byref(f)))
+    ws.last_flags = f.value
+    _warn_flags(f.value, maxnb)
+    return ws
+
+
+def target_objective(X, xc, yc, sigma):
+    """target_objective(X, xc, yc, sigma) (src/driver.jl:219-234): J and dJ/dX_T."""
+    X = np.asarray(X)
+    T = X.dtype.type
+    dx = X[0] - T(xc)
+    dy = X[1] - T(yc)
+    s2 = T(sigma) ** 2
+    e = np.exp(-(dx * dx + dy * dy) / (2 * s2))
+    J = -np.sum(e, dtype=X.dtype)
+    seed = np.stack([e * dx / s2, e * dy / s2])
+    return J, seed
+
+
+def kinetic_energy_right_half(X, V, p: SPHParams):
+    """J = sum_i 1/2 m |v_i|^2 over particles with x_i > Lx/2, and its seeds
+    (dJ/dX_T = 0 almost everywhere, dJ/dV_T = m v_i on the right half)."""
+    X, V = np.asarray(X), np.asarray(V)
+    right = X[0] > p.Lx / 2
+    J = float(0.5 * p.m * np.sum((V[0] ** 2 + V[1] ** 2)[right]))
+    seedV = np.where(right, p.m * V, 0.0).astype(V.dtype)
+    return J, np.zeros_like(X), seedV
+
+
+def launch_count() -> int:
+    return int(L.load().sph_launch_count())
+
+
+def synchronize():
+    L.check(L.load().sph_synchronize())

@@ -1,0 +1,478 @@
+// C ABI of the library, the shared runtime (stream, launch counter, kernel
+// timers) and the binomial checkpoint schedule. Precision-specific work is
+// done by the engines in sph_f32.cu / sph_f64.cu behind sph_iface.hpp.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sphadjoint_gb300.h"
+#include "sph_iface.hpp"
+
+namespace sphgb {
+
+// ---------------------------------------------------------------------------
+// runtime
+// ---------------------------------------------------------------------------
+namespace {
+thread_local std::string g_err;
+cudaStream_t g_stream = nullptr;
+bool g_stream_external = false;
+std::atomic<long long> g_launches{0};
+
+struct KTimer {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    size_t used = 0;
+    int64_t launches = 0;
+};
+KTimer g_timer[K_COUNT];
+} // namespace
+
+void cuda_check(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw Error(ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+    }
+}
+
+cudaStream_t rt_stream()
+{
+    if (!g_stream && !g_stream_external)
+        cuda_check(cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    return g_stream;
+}
+
+void rt_set_stream(cudaStream_t s)
+{
+    g_stream = s;
+    g_stream_external = s != nullptr;
+}
+
+static cudaEvent_t timer_event(KTimer &t)
+{
+    if (t.used == t.pool.size()) {
+        cudaEvent_t e;
+        cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+        t.pool.push_back(e);
+    }
+    return t.pool[t.used++];
+}
+
+void rt_before_launch(int kid)
+{
+    KTimer &t = g_timer[kid];
+    if (t.on) cuda_check(cudaEventRecord(timer_event(t), rt_stream()), "cudaEventRecord");
+}
+
+void rt_after_launch(int kid)
+{
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    KTimer &t = g_timer[kid];
+    if (t.on) {
+        cuda_check(cudaEventRecord(timer_event(t), rt_stream()), "cudaEventRecord");
+        t.launches += 1;
+    }
+}
+
+void rt_check_launch(const char *name) { cuda_check(cudaGetLastError(), name); }
+
+// ---------------------------------------------------------------------------
+// Binomial checkpointing (Griewank's revolve bound). With c snapshot slots and
+// t the smallest integer with binom(c + t, t) >= l, reversing l steps needs
+// t*l - binom(c + t, t - 1) forward steps, and no schedule needs fewer.
+// ---------------------------------------------------------------------------
+static int64_t binom_sat(int64_t n, int64_t k)
+{
+    // binom(n, k) saturating at 2^62
+    if (k < 0 || k > n) return 0;
+    k = std::min(k, n - k);
+    const long double cap = 4.611686018427387904e18L;
+    long double r = 1;
+    for (int64_t i = 1; i <= k; ++i) {
+        r = r * (long double)(n - k + i) / (long double)i;
+        if (r >= cap) return (int64_t)4611686018427387904LL;
+    }
+    return (int64_t)std::llround((double)r);
+}
+
+int64_t plan_cost(int64_t l, int64_t c)
+{
+    if (l <= 1) return 0;
+    if (c <= 1) return l * (l - 1) / 2;
+    int64_t t = 0;
+    while (binom_sat(c + t, t) < l) ++t;
+    return t * l - binom_sat(c + t, t - 1);
+}
+
+int64_t plan_split(int64_t l, int64_t c)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int64_t, int64_t>, int64_t> memo;
+    if (l <= 1) return 0;
+    if (c <= 1) return 1;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        auto it = memo.find({l, c});
+        if (it != memo.end()) return it->second;
+    }
+    int64_t best = 1, bestCost = INT64_MAX;
+    for (int64_t m = 1; m < l; ++m) {
+        const int64_t v = m + plan_cost(l - m, c - 1) + plan_cost(m, c);
+        if (v < bestCost) {
+            bestCost = v;
+            best = m;
+        }
+    }
+    std::lock_guard<std::mutex> g(mu);
+    memo[{l, c}] = best;
+    return best;
+}
+
+std::vector<int64_t> plan_descent(int64_t l, int64_t c)
+{
+    std::vector<int64_t> pos{0};
+    int64_t p = 0, len = l;
+    while (len > 1 && c >= 2) {
+        const int64_t m = plan_split(len, c);
+        p += m;
+        len -= m;
+        c -= 1;
+        pos.push_back(p);
+    }
+    return pos;
+}
+
+} // namespace sphgb
+
+using namespace sphgb;
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+template <typename F> static int32_t guarded(F &&f)
+{
+    try {
+        f();
+        return SPH_OK;
+    } catch (const Error &e) {
+        g_err = e.what();
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        g_err = "host allocation failed";
+        return SPH_ERR_NOMEM;
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return SPH_ERR_STATE;
+    }
+}
+
+static Params to_params(const sph_params *p)
+{
+    if (!p) throw Error(ERR_ARG, "params is NULL");
+    Params q;
+    q.h = p->h; q.m = p->m; q.rho0 = p->rho0; q.c = p->c; q.mu = p->mu; q.gx = p->gx;
+    q.gy = p->gy; q.dt = p->dt; q.Lx = p->Lx; q.Ly = p->Ly; q.kw = p->kw;
+    q.ngx = p->ngx; q.ngy = p->ngy;
+    return q;
+}
+
+static void need(const void *h, const char *what)
+{
+    if (!h) throw Error(ERR_ARG, std::string(what) + " is NULL");
+}
+
+static void check_dtype(int32_t d)
+{
+    if (d != SPH_F64 && d != SPH_F32) throw Error(ERR_DTYPE, "dtype must be SPH_F64 or SPH_F32");
+}
+
+#define ST(x) reinterpret_cast<StateI *>(x)
+#define TP(x) reinterpret_cast<TapeI *>(x)
+#define WS(x) reinterpret_cast<WorkI *>(x)
+#define FD(x) reinterpret_cast<FieldI *>(x)
+
+extern "C" {
+
+SPH_API const char *sph_last_error(void) { return g_err.c_str(); }
+SPH_API int32_t sph_version(void) { return 100; }
+
+SPH_API int32_t sph_set_stream(void *s)
+{
+    return guarded([&] { rt_set_stream((cudaStream_t)s); });
+}
+
+SPH_API int32_t sph_synchronize(void)
+{
+    return guarded([&] { cuda_check(cudaStreamSynchronize(rt_stream()), "synchronize"); });
+}
+
+SPH_API int32_t sph_field_create(int32_t ngx, int32_t ngy, int32_t dtype, const void *theta,
+                                 sph_field *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        FieldI *f = dtype == SPH_F64 ? make_field_f64(ngx, ngy, theta)
+                                     : make_field_f32(ngx, ngy, theta);
+        *out = reinterpret_cast<sph_field>(f);
+    });
+}
+
+SPH_API int32_t sph_field_upload(sph_field th, const void *theta)
+{
+    return guarded([&] {
+        need(th, "theta");
+        need(theta, "host theta");
+        FD(th)->upload(theta);
+    });
+}
+
+SPH_API int32_t sph_field_upload_device(sph_field th, const void *theta)
+{
+    return guarded([&] {
+        need(th, "theta");
+        need(theta, "device theta");
+        FD(th)->upload_device(theta);
+    });
+}
+
+SPH_API int32_t sph_field_destroy(sph_field th)
+{
+    return guarded([&] { delete FD(th); });
+}
+
+SPH_API int32_t sph_state_create(const sph_params *p, int64_t N, const void *X0, const void *V0,
+                                 int32_t dtype, double skin, int32_t interval, int32_t maxnb,
+                                 sph_state *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        const Params q = to_params(p);
+        NLOpts o{skin, interval, maxnb};
+        StateI *s = dtype == SPH_F64 ? make_state_f64(q, N, X0, V0, o)
+                                     : make_state_f32(q, N, X0, V0, o);
+        *out = reinterpret_cast<sph_state>(s);
+    });
+}
+
+SPH_API int32_t sph_state_destroy(sph_state st)
+{
+    return guarded([&] { delete ST(st); });
+}
+
+SPH_API int32_t sph_state_set(sph_state st, const void *X, const void *V)
+{
+    return guarded([&] { need(st, "state"); ST(st)->set(X, V); });
+}
+
+SPH_API int32_t sph_state_get(sph_state st, void *X, void *V)
+{
+    return guarded([&] { need(st, "state"); ST(st)->get(X, V); });
+}
+
+SPH_API int32_t sph_state_fields(sph_state st, void *rho, void *pterm, void *invrho, void *a,
+                                 void *alpha)
+{
+    return guarded([&] { need(st, "state"); ST(st)->fields(rho, pterm, invrho, a, alpha); });
+}
+
+SPH_API int32_t sph_state_keep_accel(sph_state st, int32_t on)
+{
+    return guarded([&] { need(st, "state"); ST(st)->keep_accel(on != 0); });
+}
+
+SPH_API int32_t sph_state_take_flags(sph_state st, uint32_t *flags)
+{
+    return guarded([&] {
+        need(st, "state");
+        const uint32_t f = ST(st)->take_flags();
+        if (flags) *flags = f;
+    });
+}
+
+SPH_API int32_t sph_state_grid(sph_state st, int32_t *nx, int32_t *ny, double *cs, int64_t *age)
+{
+    return guarded([&] { need(st, "state"); ST(st)->grid(nx, ny, cs, age); });
+}
+
+SPH_API int32_t sph_build_cells(sph_state st)
+{
+    return guarded([&] { need(st, "state"); ST(st)->build_cells(); });
+}
+
+SPH_API int32_t sph_build_neighbors(sph_state st)
+{
+    return guarded([&] { need(st, "state"); ST(st)->build_neighbors(); });
+}
+
+SPH_API int32_t sph_get_celllist(sph_state st, int32_t *counts, int32_t *starts, int32_t *order)
+{
+    return guarded([&] { need(st, "state"); ST(st)->celllist(counts, starts, order); });
+}
+
+SPH_API int32_t sph_get_neighbors(sph_state st, int32_t *indices, int32_t *nbcount)
+{
+    return guarded([&] { need(st, "state"); ST(st)->neighbors(indices, nbcount); });
+}
+
+SPH_API int32_t sph_step(sph_state st, sph_field theta, const sph_params *p)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(theta, "theta");
+        Params q;
+        if (p) q = to_params(p);
+        ST(st)->step(FD(theta), p ? &q : nullptr);
+    });
+}
+
+SPH_API int32_t sph_simulate(sph_state st, sph_field theta, const sph_params *p, int64_t nsteps,
+                             sph_tape tape, uint32_t *flags)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(theta, "theta");
+        if (nsteps < 0) throw Error(ERR_ARG, "nsteps must be >= 0");
+        Params q;
+        if (p) q = to_params(p);
+        ST(st)->simulate(FD(theta), p ? &q : nullptr, nsteps, tape ? TP(tape) : nullptr);
+        const uint32_t f = ST(st)->take_flags();
+        if (flags) *flags = f;
+    });
+}
+
+SPH_API int32_t sph_tape_create(int64_t N, int64_t nsteps, int32_t dtype, sph_tape *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        TapeI *t = dtype == SPH_F64 ? make_tape_f64(N, nsteps, 0) : make_tape_f32(N, nsteps, 0);
+        *out = reinterpret_cast<sph_tape>(t);
+    });
+}
+
+SPH_API int32_t sph_tape_create_checkpointed(int64_t N, int64_t nsteps, int32_t nsnapshots,
+                                             int32_t dtype, sph_tape *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        if (nsnapshots < 1) throw Error(ERR_ARG, "need at least one snapshot slot");
+        TapeI *t = dtype == SPH_F64 ? make_tape_f64(N, nsteps, nsnapshots)
+                                    : make_tape_f32(N, nsteps, nsnapshots);
+        *out = reinterpret_cast<sph_tape>(t);
+    });
+}
+
+SPH_API int32_t sph_tape_destroy(sph_tape tp)
+{
+    return guarded([&] { delete TP(tp); });
+}
+
+SPH_API int32_t sph_tape_reset(sph_tape tp)
+{
+    return guarded([&] { need(tp, "tape"); TP(tp)->reset(); });
+}
+
+SPH_API int32_t sph_tape_length(sph_tape tp, int64_t *n)
+{
+    return guarded([&] { need(tp, "tape"); need(n, "n"); *n = TP(tp)->length(); });
+}
+
+SPH_API int32_t sph_tape_get(sph_tape tp, int64_t n, void *X, void *V)
+{
+    return guarded([&] { need(tp, "tape"); TP(tp)->get(n, X, V); });
+}
+
+SPH_API int32_t sph_tape_recomputed_steps(sph_tape tp, int64_t *n)
+{
+    return guarded([&] { need(tp, "tape"); need(n, "n"); *n = TP(tp)->forward_steps(); });
+}
+
+SPH_API int32_t sph_workspace_create(int64_t N, const sph_params *p, int32_t dtype,
+                                     sph_workspace *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        const Params q = to_params(p);
+        WorkI *w = dtype == SPH_F64 ? make_work_f64(N, q) : make_work_f32(N, q);
+        *out = reinterpret_cast<sph_workspace>(w);
+    });
+}
+
+SPH_API int32_t sph_workspace_destroy(sph_workspace ws)
+{
+    return guarded([&] { delete WS(ws); });
+}
+
+SPH_API int32_t sph_backward(sph_workspace ws, sph_tape tp, sph_field theta, const sph_params *p,
+                             const void *seedX, const void *seedV, sph_state scratch, double skin,
+                             int32_t interval, int32_t maxnb, uint32_t *flags)
+{
+    return guarded([&] {
+        need(ws, "workspace");
+        need(tp, "tape");
+        need(theta, "theta");
+        const Params q = to_params(p);
+        NLOpts o{skin, interval, maxnb};
+        if (o.interval < 1 || o.maxnb < 1) throw Error(ERR_ARG, "interval and maxnb must be positive");
+        uint32_t f = 0;
+        WS(ws)->backward(TP(tp), FD(theta), &q, seedX, seedV, scratch ? ST(scratch) : nullptr, o, &f);
+        if (flags) *flags = f;
+    });
+}
+
+SPH_API int32_t sph_workspace_get(sph_workspace ws, void *gX, void *gV, void *gtheta)
+{
+    return guarded([&] { need(ws, "workspace"); WS(ws)->get(gX, gV, gtheta); });
+}
+
+SPH_API int64_t sph_launch_count(void) { return (int64_t)g_launches.load(); }
+
+SPH_API int32_t sph_profile_enable(int32_t kid, int32_t on)
+{
+    return guarded([&] {
+        if (kid < 0 || kid >= K_COUNT) throw Error(ERR_ARG, "kernel id out of range");
+        g_timer[kid].on = on != 0;
+    });
+}
+
+SPH_API int32_t sph_profile_read(int32_t kid, double *total_ms, int64_t *launches)
+{
+    return guarded([&] {
+        if (kid < 0 || kid >= K_COUNT) throw Error(ERR_ARG, "kernel id out of range");
+        KTimer &t = g_timer[kid];
+        cuda_check(cudaStreamSynchronize(rt_stream()), "synchronize");
+        double ms = 0;
+        for (size_t k = 0; k + 1 < t.used; k += 2) {
+            float e = 0;
+            cuda_check(cudaEventElapsedTime(&e, t.pool[k], t.pool[k + 1]), "cudaEventElapsedTime");
+            ms += e;
+        }
+        if (total_ms) *total_ms = ms;
+        if (launches) *launches = t.launches;
+    });
+}
+
+SPH_API int32_t sph_profile_reset(void)
+{
+    return guarded([&] {
+        for (auto &t : g_timer) {
+            t.used = 0;
+            t.launches = 0;
+        }
+    });
+}
+
+SPH_API int64_t sph_plan_cost(int64_t l, int64_t c) { return plan_cost(l, c); }
+SPH_API int64_t sph_plan_split(int64_t l, int64_t c) { return plan_split(l, c); }
+
+} // extern "C"

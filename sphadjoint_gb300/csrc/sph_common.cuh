@@ -1,0 +1,214 @@
+// Shared device types and the per-pair / per-particle math of the WCSPH step.
+//
+// Every formula keeps the reference's association and constants so that the
+// FP64 build (compiled with --fmad=false, IEEE division and sqrt) reproduces
+// the reference's rounding bit for bit:
+//   Wendland C2 kernel ............ src/kernels.jl:15-44
+//   relu^2 wall and its derivative  src/params.jl:80-90
+//   bilinear design field alpha(x)  src/params.jl:98-126
+// The FP32 build uses the same source with multiply-add contraction enabled.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sphgb {
+
+template <typename T> struct vec2;
+template <> struct vec2<float> { using type = float2; };
+template <> struct vec2<double> { using type = double2; };
+template <typename T> using T2 = typename vec2<T>::type;
+
+template <typename T> __host__ __device__ __forceinline__ T2<T> mk2(T x, T y)
+{
+    T2<T> r;
+    r.x = x;
+    r.y = y;
+    return r;
+}
+
+// Products and sums that are never contracted into FMA, whatever the build
+// flags: the neighbour-list predicates must see the same r^2 in every kernel.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+
+template <typename T> __device__ __forceinline__ T r2_exact(T dx, T dy)
+{
+    return add_rn(mul_rn(dx, dx), mul_rn(dy, dy));
+}
+
+// SPHParams{T} (src/params.jl:58-72) plus the constants each reference kernel
+// forms from it, formed on the host in T with the same association:
+//   A = T(7)/(T(4)*T(pi)*h^2), invh = 1/h, r2max = T(4)*h*h,
+//   Fc = -5*A*invh*invh, Gc = T(7.5)*A*invh*invh, twomumass = 2*m*mu,
+//   c2 = c^2, hxg = Lx/(ngx-1), gxmax = T(ngx-1) - T(1e-6).
+template <typename T> struct Phys {
+    T h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
+    int ngx, ngy;
+    T A, invh, r2max, Fc, Gc, twomumass, c2;
+    T hxg, hyg, ngx1, ngy1, gxmax, gymax;
+};
+
+// Everything a neighbour loop needs about the particle system: positions in
+// cell order, the neighbour masks and the cell table of the last rebuild.
+template <typename T> struct NLView {
+    int64_t N;
+    int nx, ny;
+    int maxnb;
+    T rc2, r2min;
+    const T2<T> *pos;
+    const T2<T> *xref;
+    const uint32_t *center;   // cx | cy << 16 | spill << 31 (1-based cx, cy)
+    const uint64_t *masks;    // 3 rows, slot-major: masks[r * N + i]
+    const int32_t *cellStart; // ncell + 1 exclusive offsets
+};
+
+// Visit the neighbours of particle i in the reference's scan order
+// (src/neighbors.jl:217-244): cell rows ddy = -1..1, within a row cells
+// ddx = -1..1, within a cell ascending particle id. Because particles are
+// stored sorted by (cell, id), each row is one contiguous slot range and the
+// order is simply ascending slot. The fast path walks the bits of one 64-bit
+// mask per row. A particle whose row range exceeds 64 slots is "spilled": it
+// re-evaluates the rebuild-time predicate r2min < r^2 < rc^2 on the stored
+// rebuild positions and truncates at maxnb, which is exactly what the
+// reference's fixed-length neighbour rows hold.
+template <typename T, typename F>
+__device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, int64_t i, F &&f)
+{
+    const uint32_t cc = v.center[i];
+    const int cx = (int)(cc & 0xffffu);
+    const int cy = (int)((cc >> 16) & 0x7fffu);
+    const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
+    if (!(cc >> 31)) {
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            uint64_t m = v.masks[(int64_t)r * v.N + i];
+            if (m) {
+                const int jy = cy + r - 1;
+                const int64_t b = v.cellStart[(int64_t)(jx0 - 1) + (int64_t)(jy - 1) * v.nx];
+                do {
+                    const int k = __ffsll((long long)m) - 1;
+                    m &= m - 1;
+                    f(b + k);
+                } while (m);
+            }
+        }
+    } else {
+        const int jx1 = cx + 1 < v.nx ? cx + 1 : v.nx;
+        const T2<T> xr = v.xref[i];
+        int cnt = 0;
+        for (int r = 0; r < 3; ++r) {
+            const int jy = cy + r - 1;
+            if (jy < 1 || jy > v.ny) continue;
+            const int64_t row = (int64_t)(jy - 1) * v.nx;
+            const int64_t b = v.cellStart[row + jx0 - 1];
+            const int64_t e = v.cellStart[row + jx1];
+            for (int64_t j = b; j < e; ++j) {
+                const T2<T> xj = v.xref[j];
+                const T r2 = r2_exact<T>(sub_rn(xr.x, xj.x), sub_rn(xr.y, xj.y));
+                if (v.r2min < r2 && r2 < v.rc2) {
+                    if (cnt < v.maxnb) {
+                        ++cnt;
+                        f(j);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// clamp(unsafe_trunc(Int, floor(v)) + 2, 1, n) (src/neighbors.jl:38-42,217-218).
+// The float clamp keeps the conversion defined; no finite result changes.
+template <typename T> __host__ __device__ __forceinline__ int cell_coord(T v, int n)
+{
+    T f = floor(v);
+    if (!(f > (T)(-4))) f = (T)(-4);
+    if (f > (T)(n + 4)) f = (T)(n + 4);
+    int c = (int)f + 2;
+    c = c < 1 ? 1 : c;
+    return c > n ? n : c;
+}
+
+// wall_accel / wall_daccel (src/params.jl:80-90); max(zero(T), -x) keeps +0.
+template <typename T> __device__ __forceinline__ T wall_accel(T x, T L, T kw)
+{
+    const T lo = (-x > (T)0) ? -x : (T)0;
+    const T hi = (x - L > (T)0) ? x - L : (T)0;
+    return kw * (lo * lo - hi * hi);
+}
+
+template <typename T> __device__ __forceinline__ T wall_daccel(T x, T L, T kw)
+{
+    const T lo = (-x > (T)0) ? -x : (T)0;
+    const T hi = (x - L > (T)0) ? x - L : (T)0;
+    return kw * ((T)(-2) * lo - (T)2 * hi);
+}
+
+// interp_cell (src/params.jl:98-112), 0-based i0, j0.
+template <typename T>
+__device__ __forceinline__ void interp_cell(T x, T y, const Phys<T> &p, int &i0, int &j0, T &fx,
+                                            T &fy, T &ax, T &ay)
+{
+    const T gx = x / p.hxg;
+    const T gy = y / p.hyg;
+    ax = ((gx > (T)0) & (gx < p.ngx1)) ? (T)1 : (T)0;
+    ay = ((gy > (T)0) & (gy < p.ngy1)) ? (T)1 : (T)0;
+    const T gxc = gx > p.gxmax ? p.gxmax : (gx < (T)0 ? (T)0 : gx);
+    const T gyc = gy > p.gymax ? p.gymax : (gy < (T)0 ? (T)0 : gy);
+    const T fgx = floor(gxc), fgy = floor(gyc);
+    int a = (fgx == fgx) ? (int)fgx : 0;
+    int b = (fgy == fgy) ? (int)fgy : 0;
+    a = a < 0 ? 0 : (a > p.ngx - 2 ? p.ngx - 2 : a);
+    b = b < 0 ? 0 : (b > p.ngy - 2 ? p.ngy - 2 : b);
+    i0 = a;
+    j0 = b;
+    fx = gxc - (T)a;
+    fy = gyc - (T)b;
+}
+
+// interp_alpha (src/params.jl:115-126); theta is (ngy, ngx) column-major.
+template <typename T>
+__device__ __forceinline__ void interp_alpha(const T *theta, T x, T y, const Phys<T> &p, T &a,
+                                             T &dadx, T &dady)
+{
+    int i0, j0;
+    T fx, fy, ax, ay;
+    interp_cell(x, y, p, i0, j0, fx, fy, ax, ay);
+    const int64_t l00 = (int64_t)j0 + (int64_t)i0 * p.ngy;
+    const T t00 = __ldg(theta + l00);
+    const T t01 = __ldg(theta + l00 + p.ngy);
+    const T t10 = __ldg(theta + l00 + 1);
+    const T t11 = __ldg(theta + l00 + p.ngy + 1);
+    a = ((T)1 - fx) * ((T)1 - fy) * t00 + fx * ((T)1 - fy) * t01 + ((T)1 - fx) * fy * t10 +
+        fx * fy * t11;
+    dadx = (((T)1 - fy) * (t01 - t00) + fy * (t11 - t10)) / p.hxg * ax;
+    dady = (((T)1 - fx) * (t10 - t00) + fx * (t11 - t01)) / p.hyg * ay;
+}
+
+template <typename T> __device__ __forceinline__ T interp_alpha_value(const T *theta, T x, T y,
+                                                                      const Phys<T> &p)
+{
+    int i0, j0;
+    T fx, fy, ax, ay;
+    interp_cell(x, y, p, i0, j0, fx, fy, ax, ay);
+    const int64_t l00 = (int64_t)j0 + (int64_t)i0 * p.ngy;
+    const T t00 = __ldg(theta + l00);
+    const T t01 = __ldg(theta + l00 + p.ngy);
+    const T t10 = __ldg(theta + l00 + 1);
+    const T t11 = __ldg(theta + l00 + p.ngy + 1);
+    return ((T)1 - fx) * ((T)1 - fy) * t00 + fx * ((T)1 - fy) * t01 + ((T)1 - fx) * fy * t10 +
+           fx * fy * t11;
+}
+
+// Status bits kept in a device word and returned at the API boundary.
+enum : uint32_t {
+    FLAG_NL_OVERFLOW = 1u,     // a neighbour row exceeded maxnb (reference flags[1])
+    FLAG_DISPLACEMENT = 2u,    // displacement since rebuild > skin*h (reference flags[2])
+    FLAG_NONFINITE = 4u,       // a non-finite position or velocity was produced
+};
+
+} // namespace sphgb

@@ -1,0 +1,895 @@
+// Host side of the engine, one instantiation per precision.
+//
+//   Sys<T>    State: particles in cell order + cell list + neighbour masks
+//             (src/driver.jl:5-36, src/neighbors.jl:9-36,150-190)
+//   Tape<T>   Tape: full (X, V) history (src/driver.jl:45-83), or a binomial
+//             checkpoint tape that keeps a fixed number of snapshots and
+//             recomputes the rest during the reverse sweep
+//   Work<T>   AdjointWorkspace + backward! (src/driver.jl:117-207)
+//   Field<T>  the design field theta on the device
+//
+// Every public call is enqueued on the library stream; calls that return data
+// to the host synchronise, like the reference's synchronize at its API exits.
+#pragma once
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <functional>
+#include <limits>
+#include <memory>
+#include <utility>
+#include <vector>
+
+#include "sph_iface.hpp"
+#include "sph_kernels.cuh"
+
+namespace sphgb {
+
+template <typename T> struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() {}
+    explicit DevBuf(size_t count) { alloc(count); }
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf &operator=(DevBuf &&o) noexcept
+    {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    ~DevBuf() { release(); }
+    void alloc(size_t count)
+    {
+        release();
+        n = count;
+        if (count) {
+            cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * count);
+            if (e != cudaSuccess) {
+                p = nullptr;
+                n = 0;
+                (void)cudaGetLastError();
+                throw Error(e == cudaErrorMemoryAllocation ? ERR_NOMEM : ERR_CUDA,
+                            std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+            }
+        }
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    size_t bytes() const { return sizeof(T) * n; }
+    void zero() { if (n) SPH_CK(cudaMemsetAsync(p, 0, bytes(), rt_stream())); }
+    void copy_from(const DevBuf &o) { if (n) SPH_CK(cudaMemcpyAsync(p, o.p, bytes(), cudaMemcpyDeviceToDevice, rt_stream())); }
+};
+
+inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
+
+#define SPH_LAUNCH(kid, kern, n, ...)                                                         \
+    do {                                                                                      \
+        if ((n) > 0) {                                                                        \
+            ::sphgb::rt_before_launch(kid);                                                   \
+            kern<<<::sphgb::grid_for(n), ::sphgb::kBlock, 0, ::sphgb::rt_stream()>>>(__VA_ARGS__); \
+            ::sphgb::rt_after_launch(kid);                                                    \
+        }                                                                                     \
+    } while (0)
+
+// Constants formed in T exactly as the reference kernels form them.
+template <typename T> Phys<T> make_phys(const Params &q)
+{
+    Phys<T> p;
+    p.h = (T)q.h; p.m = (T)q.m; p.rho0 = (T)q.rho0; p.c = (T)q.c; p.mu = (T)q.mu;
+    p.gx = (T)q.gx; p.gy = (T)q.gy; p.dt = (T)q.dt; p.Lx = (T)q.Lx; p.Ly = (T)q.Ly;
+    p.kw = (T)q.kw; p.ngx = q.ngx; p.ngy = q.ngy;
+    const T pi = (T)3.14159265358979323846;
+    p.A = (T)7 / ((T)4 * pi * (p.h * p.h));
+    p.invh = (T)1 / p.h;
+    p.r2max = (T)4 * p.h * p.h;
+    p.Fc = (T)(-5) * p.A * p.invh * p.invh;
+    p.Gc = (T)7.5 * p.A * p.invh * p.invh;
+    p.twomumass = (T)2 * p.m * p.mu;
+    p.c2 = p.c * p.c;
+    p.ngx1 = (T)(q.ngx - 1);
+    p.ngy1 = (T)(q.ngy - 1);
+    p.hxg = p.Lx / p.ngx1;
+    p.hyg = p.Ly / p.ngy1;
+    p.gxmax = p.ngx1 - (T)1e-6;
+    p.gymax = p.ngy1 - (T)1e-6;
+    return p;
+}
+
+inline void check_params(const Params &p)
+{
+    if (!(p.h > 0)) throw Error(ERR_ARG, "h must be positive");
+    if (p.ngx < 2 || p.ngy < 2) throw Error(ERR_ARG, "ngx and ngy must be at least 2");
+}
+
+// exclusive scan of n int32 -> out[0..n] (+ optional copy); tmp >= blocks
+inline void scan_excl(const int32_t *in, int64_t n, int32_t *out, int32_t *out2, int32_t *tmp)
+{
+    const int64_t nb = (n + kScanTile - 1) / kScanTile;
+    if (nb <= 1) {
+        rt_before_launch(K_SCAN);
+        k_scan_down<<<1, kBlock, 0, rt_stream()>>>(in, n, nullptr, out, out2);
+        rt_after_launch(K_SCAN);
+        return;
+    }
+    rt_before_launch(K_SCAN);
+    k_scan_reduce<<<(unsigned)nb, kBlock, 0, rt_stream()>>>(in, n, tmp);
+    k_scan_top<<<1, 1024, 0, rt_stream()>>>(tmp, nb);
+    k_scan_down<<<(unsigned)nb, kBlock, 0, rt_stream()>>>(in, n, tmp, out, out2);
+    rt_after_launch(K_SCAN);
+}
+
+template <typename T> class Field final : public FieldI {
+  public:
+    int nx_, ny_;
+    DevBuf<T> th;
+    DevBuf<double> stage;
+    Field(int ngx, int ngy, const void *host) : nx_(ngx), ny_(ngy), th((size_t)ngx * ngy)
+    {
+        if (ngx < 2 || ngy < 2) throw Error(ERR_ARG, "theta must be at least 2 x 2");
+        if (host) upload(host); else th.zero();
+    }
+    int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
+    int ngx() const override { return nx_; }
+    int ngy() const override { return ny_; }
+    void upload(const void *host) override
+    {
+        SPH_CK(cudaMemcpyAsync(th.p, host, th.bytes(), cudaMemcpyHostToDevice, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+    }
+    void upload_device(const void *dev) override
+    {
+        SPH_CK(cudaMemcpyAsync(th.p, dev, th.bytes(), cudaMemcpyDeviceToDevice, rt_stream()));
+    }
+};
+
+// A copy of everything that determines the future of a Sys: the state in
+// cell order, its permutation, and the neighbour structure of the last
+// rebuild (so recomputation from a snapshot repeats the forward bit for bit).
+template <typename T> struct Snap {
+    DevBuf<T2<T>> pos, vel, xref;
+    DevBuf<int32_t> perm, invperm, cellStart, nbcount;
+    DevBuf<uint32_t> center;
+    DevBuf<uint64_t> masks;
+    int64_t age = INT64_MAX;
+    bool valid = false;
+};
+
+template <typename T> class Sys final : public StateI {
+  public:
+    Params prm;
+    int64_t N_;
+    int nx, ny;
+    int64_t ncell;
+    double cs_d, rc_d, dmax_d;
+    NLOpts opts;
+    int64_t age = INT64_MAX;
+    T cs, invcs, rc2, r2min, dmax2;
+    DevBuf<T2<T>> pos[2], vel[2];
+    int cur = 0;
+    DevBuf<T2<T>> xref;
+    DevBuf<int32_t> perm, invperm, cellStart, nbcount, cellTmp, counts, cursor, bucketSrc,
+        bucketId, scanTmp;
+    DevBuf<uint32_t> center, flags;
+    DevBuf<uint64_t> masks;
+    DevBuf<T> rho;
+    DevBuf<T2<T>> prho;
+    DevBuf<T2<T>> accOut;
+    DevBuf<T> alphaOut;
+    DevBuf<T2<T>> stage2;
+    DevBuf<T> stage1;
+    DevBuf<int32_t> clStart, clOrder; // build! without a neighbour rebuild
+    bool cellsOnlyLatest = false;
+    bool keepAccel = false;
+
+    Sys(const Params &p, int64_t N, const void *X0, const void *V0, NLOpts o)
+        : prm(p), N_(N), opts(o)
+    {
+        check_params(p);
+        if (N < 0 || N > (int64_t)INT32_MAX - 1) throw Error(ERR_ARG, "particle count out of range");
+        if (o.maxnb < 1) throw Error(ERR_ARG, "maxnb must be positive");
+        if (o.interval < 1) throw Error(ERR_ARG, "interval must be positive");
+        // NeighborList: rc = Float64(support(p)) * (1 + skin), dmax = Float64(h) * skin
+        const T hT = (T)p.h;
+        const T support = (T)2 * hT;
+        rc_d = (double)support * (1.0 + o.skin);
+        dmax_d = (double)hT * o.skin;
+        // CellList(backend, N, p; cs = nl.rc)
+        cs_d = rc_d;
+        const double LxT = (double)(T)p.Lx, LyT = (double)(T)p.Ly;
+        nx = (int)std::max(1.0, std::ceil(LxT / cs_d) + 2);
+        ny = (int)std::max(1.0, std::ceil(LyT / cs_d) + 2);
+        if (!(cs_d > 0) || nx > 65535 || ny > 32767)
+            throw Error(ERR_ARG, "cell grid too large (nx <= 65535, ny <= 32767)");
+        ncell = (int64_t)nx * ny;
+        cs = (T)cs_d;
+        invcs = (T)1 / cs;
+        rc2 = (T)(rc_d * rc_d);
+        r2min = std::numeric_limits<T>::epsilon() * hT * hT;
+        dmax2 = (T)(dmax_d * dmax_d);
+        const size_t n1 = (size_t)std::max<int64_t>(N, 1);
+        for (int k = 0; k < 2; ++k) {
+            pos[k].alloc(n1);
+            vel[k].alloc(n1);
+        }
+        xref.alloc(n1);
+        perm.alloc(n1);
+        invperm.alloc(n1);
+        cellStart.alloc((size_t)ncell + 1);
+        nbcount.alloc(n1);
+        cellTmp.alloc(n1);
+        counts.alloc((size_t)ncell);
+        cursor.alloc((size_t)ncell);
+        bucketSrc.alloc(n1);
+        bucketId.alloc(n1);
+        scanTmp.alloc((size_t)((ncell + kScanTile - 1) / kScanTile + 1));
+        center.alloc(n1);
+        flags.alloc(1);
+        masks.alloc(3 * n1);
+        rho.alloc(n1);
+        prho.alloc(n1);
+        stage2.alloc(n1);
+        stage1.alloc(n1);
+        flags.zero();
+        xref.zero();
+        masks.zero();
+        center.zero();
+        cellStart.zero();
+        init_identity();
+        if (X0 || V0) set(X0, V0);
+        else {
+            pos[0].zero();
+            vel[0].zero();
+        }
+    }
+
+    int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
+    int64_t N() const override { return N_; }
+
+    void init_identity()
+    {
+        std::vector<int32_t> id((size_t)std::max<int64_t>(N_, 1));
+        for (int64_t i = 0; i < N_; ++i) id[i] = (int32_t)i;
+        if (N_) {
+            SPH_CK(cudaMemcpyAsync(perm.p, id.data(), sizeof(int32_t) * N_, cudaMemcpyHostToDevice, rt_stream()));
+            SPH_CK(cudaMemcpyAsync(invperm.p, id.data(), sizeof(int32_t) * N_, cudaMemcpyHostToDevice, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
+    }
+
+    NLView<T> view() const
+    {
+        NLView<T> v;
+        v.N = N_;
+        v.nx = nx;
+        v.ny = ny;
+        v.maxnb = opts.maxnb;
+        v.rc2 = rc2;
+        v.r2min = r2min;
+        v.pos = pos[cur].p;
+        v.xref = xref.p;
+        v.center = center.p;
+        v.masks = masks.p;
+        v.cellStart = cellStart.p;
+        return v;
+    }
+
+    // host (id order, interleaved T) -> cell order
+    void set(const void *X, const void *V) override
+    {
+        if (!N_) return;
+        if (X) {
+            SPH_CK(cudaMemcpyAsync(stage2.p, X, stage2.bytes(), cudaMemcpyHostToDevice, rt_stream()));
+            SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, perm.p, stage2.p, pos[cur].p);
+        }
+        if (V) {
+            SPH_CK(cudaMemcpyAsync(stage2.p, V, stage2.bytes(), cudaMemcpyHostToDevice, rt_stream()));
+            SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, perm.p, stage2.p, vel[cur].p);
+        }
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+    }
+
+    void get(void *X, void *V) override
+    {
+        if (!N_) return;
+        if (X) {
+            SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, perm.p, pos[cur].p, stage2.p);
+            SPH_CK(cudaMemcpyAsync(X, stage2.p, stage2.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
+        if (V) {
+            SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, perm.p, vel[cur].p, stage2.p);
+            SPH_CK(cudaMemcpyAsync(V, stage2.p, stage2.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
+    }
+
+    void get1(const T *src, void *out)
+    {
+        SPH_LAUNCH(K_MISC, k_scatter_to_ids1<T>, N_, N_, perm.p, src, stage1.p);
+        SPH_CK(cudaMemcpyAsync(out, stage1.p, stage1.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+    }
+
+    void fields(void *rhoOut, void *ptermOut, void *invrhoOut, void *aOut, void *alOut) override
+    {
+        if (!N_) return;
+        if (rhoOut) get1(rho.p, rhoOut);
+        if (ptermOut || invrhoOut) {
+            std::vector<T> tmp(2 * (size_t)N_);
+            SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, perm.p, prho.p, stage2.p);
+            SPH_CK(cudaMemcpyAsync(tmp.data(), stage2.p, stage2.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+            for (int64_t i = 0; i < N_; ++i) {
+                if (ptermOut) ((T *)ptermOut)[i] = tmp[2 * i];
+                if (invrhoOut) ((T *)invrhoOut)[i] = tmp[2 * i + 1];
+            }
+        }
+        if (aOut) {
+            if (!accOut.p) throw Error(ERR_STATE, "accelerations are kept only after keep_accel(1)");
+            SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, perm.p, accOut.p, stage2.p);
+            SPH_CK(cudaMemcpyAsync(aOut, stage2.p, stage2.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
+        if (alOut) {
+            if (!alphaOut.p) throw Error(ERR_STATE, "alpha is kept only after keep_accel(1)");
+            get1(alphaOut.p, alOut);
+        }
+    }
+
+    void keep_accel(bool on) override
+    {
+        keepAccel = on;
+        if (on && !accOut.p) {
+            accOut.alloc((size_t)std::max<int64_t>(N_, 1));
+            alphaOut.alloc((size_t)std::max<int64_t>(N_, 1));
+            accOut.zero();
+            alphaOut.zero();
+        }
+    }
+
+    // build_neighbors! (src/neighbors.jl:252-263): cell list, permutation of
+    // the particle data (and of up to two extra per-particle arrays) into the
+    // new cell order, neighbour masks. ex*N receive the permuted extras.
+    void rebuild(const T2<T> *ex0 = nullptr, T2<T> *ex0N = nullptr, const T2<T> *ex1 = nullptr,
+                 T2<T> *ex1N = nullptr)
+    {
+        const int check = age != INT64_MAX ? 1 : 0;
+        if (N_ > 0) {
+            counts.zero();
+            SPH_LAUNCH(K_ASSIGN, k_assign<T>, N_, N_, pos[cur].p, xref.p, check, dmax2, cs, nx, ny,
+                       cellTmp.p, counts.p, flags.p);
+            scan_excl(counts.p, ncell, cellStart.p, cursor.p, scanTmp.p);
+            SPH_LAUNCH(K_BUCKET, k_bucket, N_, N_, cellTmp.p, perm.p, cursor.p, bucketSrc.p, bucketId.p);
+            const int nxt = 1 - cur;
+            SPH_LAUNCH(K_RANK, k_rank_permute<T>, N_, N_, cellTmp.p, cellStart.p, bucketSrc.p,
+                       bucketId.p, pos[cur].p, vel[cur].p, pos[nxt].p, vel[nxt].p, xref.p, perm.p,
+                       invperm.p, ex0, ex0N, ex1, ex1N);
+            cur = nxt;
+            SPH_LAUNCH(K_NLBUILD, k_nl_build<T>, N_, N_, nx, ny, opts.maxnb, invcs, rc2, r2min,
+                       pos[cur].p, cellStart.p, center.p, masks.p, nbcount.p, flags.p);
+        }
+        age = 0;
+        cellsOnlyLatest = false;
+    }
+
+    void build_neighbors() override
+    {
+        rebuild();
+        rt_check_launch("build_neighbors");
+    }
+
+    // build! alone (src/neighbors.jl:97-114): the cell list of the current
+    // positions, without touching the particle order or the neighbour list.
+    void build_cells() override
+    {
+        if (!clStart.p) {
+            clStart.alloc((size_t)ncell + 1);
+            clOrder.alloc((size_t)std::max<int64_t>(N_, 1));
+        }
+        if (N_ > 0) {
+            counts.zero();
+            SPH_LAUNCH(K_ASSIGN, k_assign<T>, N_, N_, pos[cur].p, xref.p, 0, dmax2, cs, nx, ny,
+                       cellTmp.p, counts.p, flags.p);
+            scan_excl(counts.p, ncell, clStart.p, cursor.p, scanTmp.p);
+            SPH_LAUNCH(K_BUCKET, k_bucket, N_, N_, cellTmp.p, perm.p, cursor.p, bucketSrc.p, bucketId.p);
+            SPH_LAUNCH(K_RANK, k_rank_permute<T>, N_, N_, cellTmp.p, clStart.p, bucketSrc.p,
+                       bucketId.p, pos[cur].p, vel[cur].p, (T2<T> *)nullptr, (T2<T> *)nullptr,
+                       (T2<T> *)nullptr, clOrder.p, (int32_t *)nullptr, (const T2<T> *)nullptr,
+                       (T2<T> *)nullptr, (const T2<T> *)nullptr, (T2<T> *)nullptr);
+        } else {
+            clStart.zero();
+        }
+        cellsOnlyLatest = true;
+        rt_check_launch("build_cells");
+    }
+
+    void maybe_rebuild(const T2<T> *ex0 = nullptr, T2<T> *ex0N = nullptr,
+                       const T2<T> *ex1 = nullptr, T2<T> *ex1N = nullptr, bool *did = nullptr)
+    {
+        // maybe_rebuild! (src/neighbors.jl:273-279): test, then count
+        bool r = false;
+        if (age >= opts.interval) {
+            rebuild(ex0, ex0N, ex1, ex1N);
+            r = true;
+        }
+        age += 1;
+        if (did) *did = r;
+    }
+
+    // step! (src/forward.jl:161-173); tx/tv: optional tape slot (id order)
+    void step_impl(const T *theta, const Phys<T> &p, T2<T> *tx, T2<T> *tv)
+    {
+        maybe_rebuild();
+        if (N_ == 0) return;
+        if (tx) SPH_LAUNCH(K_TAPE, k_tape_store<T>, N_, N_, perm.p, pos[cur].p, vel[cur].p, tx, tv);
+        const NLView<T> v = view();
+        SPH_LAUNCH(K_DENSITY, k_density_eos<T>, N_, v, p, rho.p, prho.p);
+        const int nxt = 1 - cur;
+        SPH_LAUNCH(K_ACCEL_INTEGRATE, k_accel_integrate<T>, N_, v, p, vel[cur].p, prho.p, theta,
+                   pos[nxt].p, vel[nxt].p, keepAccel ? accOut.p : (T2<T> *)nullptr,
+                   keepAccel ? alphaOut.p : (T *)nullptr, flags.p);
+        cur = nxt;
+    }
+
+    Field<T> *field_of(FieldI *f)
+    {
+        auto *t = dynamic_cast<Field<T> *>(f);
+        if (!t) throw Error(ERR_DTYPE, "theta has a different precision than the state");
+        return t;
+    }
+
+    static void check_shape(const Params &q, const Field<T> *th)
+    {
+        if (q.ngx != th->nx_ || q.ngy != th->ny_)
+            throw Error(ERR_ARG, "params (ngx, ngy) do not match the theta field");
+    }
+
+    void step(FieldI *theta, const Params *p) override
+    {
+        Field<T> *th = field_of(theta);
+        const Params &q = p ? *p : prm;
+        check_params(q);
+        check_shape(q, th);
+        step_impl(th->th.p, make_phys<T>(q), nullptr, nullptr);
+        rt_check_launch("step");
+    }
+
+    void simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tape) override;
+
+    void celllist(int32_t *countsOut, int32_t *startsOut, int32_t *orderOut) override
+    {
+        const int32_t *cst = cellsOnlyLatest ? clStart.p : cellStart.p;
+        const int32_t *ord = cellsOnlyLatest ? clOrder.p : perm.p;
+        std::vector<int32_t> s((size_t)ncell + 1);
+        SPH_CK(cudaMemcpyAsync(s.data(), cst, sizeof(int32_t) * (ncell + 1), cudaMemcpyDeviceToHost, rt_stream()));
+        std::vector<int32_t> o((size_t)std::max<int64_t>(N_, 1));
+        if (N_) SPH_CK(cudaMemcpyAsync(o.data(), ord, sizeof(int32_t) * N_, cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+        if (N_ == 0) std::fill(s.begin(), s.end(), 0);
+        for (int64_t c = 0; c < ncell; ++c) {
+            if (countsOut) countsOut[c] = s[c + 1] - s[c];
+            if (startsOut) startsOut[c] = s[c];
+        }
+        if (orderOut)
+            for (int64_t i = 0; i < N_; ++i) orderOut[i] = o[i] + 1; // 1-based ids
+    }
+
+    void neighbors(int32_t *indices, int32_t *nbc) override;
+
+    uint32_t take_flags() override
+    {
+        uint32_t f = 0;
+        SPH_CK(cudaMemcpyAsync(&f, flags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+        flags.zero();
+        return f;
+    }
+
+    void grid(int32_t *nxo, int32_t *nyo, double *cso, int64_t *ageo) const override
+    {
+        if (nxo) *nxo = nx;
+        if (nyo) *nyo = ny;
+        if (cso) *cso = cs_d;
+        if (ageo) *ageo = age;
+    }
+
+    void sync() override { SPH_CK(cudaStreamSynchronize(rt_stream())); }
+
+    // ---- snapshots ----
+    void snap_alloc(Snap<T> &s) const
+    {
+        const size_t n1 = (size_t)std::max<int64_t>(N_, 1);
+        if (s.pos.p) return;
+        s.pos.alloc(n1); s.vel.alloc(n1); s.xref.alloc(n1);
+        s.perm.alloc(n1); s.invperm.alloc(n1); s.nbcount.alloc(n1);
+        s.cellStart.alloc((size_t)ncell + 1);
+        s.center.alloc(n1); s.masks.alloc(3 * n1);
+    }
+    void save(Snap<T> &s)
+    {
+        snap_alloc(s);
+        s.pos.copy_from(pos[cur]); s.vel.copy_from(vel[cur]); s.xref.copy_from(xref);
+        s.perm.copy_from(perm); s.invperm.copy_from(invperm); s.nbcount.copy_from(nbcount);
+        s.cellStart.copy_from(cellStart); s.center.copy_from(center); s.masks.copy_from(masks);
+        s.age = age;
+        s.valid = true;
+    }
+    void restore(const Snap<T> &s)
+    {
+        if (!s.valid) throw Error(ERR_STATE, "restoring an empty snapshot");
+        pos[cur].copy_from(s.pos); vel[cur].copy_from(s.vel); xref.copy_from(s.xref);
+        perm.copy_from(s.perm); invperm.copy_from(s.invperm); nbcount.copy_from(s.nbcount);
+        cellStart.copy_from(s.cellStart); center.copy_from(s.center); masks.copy_from(s.masks);
+        age = s.age;
+        cellsOnlyLatest = false;
+    }
+    bool same_config(const Sys &o) const
+    {
+        return N_ == o.N_ && nx == o.nx && ny == o.ny && opts.maxnb == o.opts.maxnb &&
+               opts.interval == o.opts.interval && rc_d == o.rc_d;
+    }
+};
+
+// List the neighbour rows in the reference's particle-major layout
+// (indices[(i-1)*maxnb + m], 1-based ids), same order as _nl_build!.
+template <typename T>
+__global__ void k_list_neighbors(NLView<T> v, const int32_t *__restrict__ perm,
+                                 int32_t *__restrict__ out, int32_t *__restrict__ nbc)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    const int32_t id = perm[i];
+    int m = 0;
+    for_each_neighbor<T>(v, i, [&](int64_t j) {
+        out[(int64_t)id * v.maxnb + m] = perm[j] + 1;
+        ++m;
+    });
+    nbc[id] = m;
+}
+
+template <typename T> void Sys<T>::neighbors(int32_t *indices, int32_t *nbc)
+{
+    if (!N_) return;
+    DevBuf<int32_t> out((size_t)N_ * opts.maxnb), cnt((size_t)N_);
+    out.zero();
+    SPH_LAUNCH(K_MISC, k_list_neighbors<T>, N_, view(), perm.p, out.p, cnt.p);
+    if (indices) SPH_CK(cudaMemcpyAsync(indices, out.p, out.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+    if (nbc) SPH_CK(cudaMemcpyAsync(nbc, cnt.p, cnt.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+    SPH_CK(cudaStreamSynchronize(rt_stream()));
+}
+
+// ---------------------------------------------------------------------------
+// Tape
+// ---------------------------------------------------------------------------
+template <typename T> class Tape final : public TapeI {
+  public:
+    int64_t N_, cap_, n_ = 0;
+    int32_t nsnap_;
+    // full history: (X, V) before every step, id order
+    DevBuf<T2<T>> hx, hv;
+    // checkpoints
+    std::vector<int64_t> descent;        // planned snapshot positions (0-based step index)
+    std::vector<std::unique_ptr<Snap<T>>> slots;
+    std::vector<int64_t> slotPos;        // position held by each slot (-1 = free)
+    std::unique_ptr<Sys<T>> recomp;      // state used to recompute during backward
+    int64_t fwdSteps = 0;
+
+    Tape(int64_t N, int64_t cap, int32_t nsnap) : N_(N), cap_(cap), nsnap_(nsnap)
+    {
+        if (N < 0 || cap < 0) throw Error(ERR_ARG, "negative tape size");
+        if (nsnap < 0) throw Error(ERR_ARG, "negative snapshot count");
+        if (nsnap == 0) {
+            const size_t n = (size_t)std::max<int64_t>(N, 1) * (size_t)std::max<int64_t>(cap, 1);
+            hx.alloc(n);
+            hv.alloc(n);
+        } else {
+            descent = plan_descent(std::max<int64_t>(cap, 1), nsnap);
+            slots.resize((size_t)nsnap);
+            slotPos.assign((size_t)nsnap, -1);
+        }
+    }
+    int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
+    int64_t N() const override { return N_; }
+    int64_t capacity() const override { return cap_; }
+    int64_t length() const override { return n_; }
+    int32_t snapshots() const override { return nsnap_; }
+    int64_t forward_steps() const override { return fwdSteps; }
+    void reset() override
+    {
+        n_ = 0;
+        std::fill(slotPos.begin(), slotPos.end(), -1);
+    }
+    void get(int64_t n, void *X, void *V) override
+    {
+        if (nsnap_) throw Error(ERR_STATE, "a checkpoint tape keeps no per-step history");
+        if (n < 1 || n > n_) throw Error(ERR_ARG, "tape index out of range");
+        const size_t off = (size_t)(n - 1) * N_;
+        if (X) SPH_CK(cudaMemcpyAsync(X, hx.p + off, sizeof(T2<T>) * N_, cudaMemcpyDeviceToHost, rt_stream()));
+        if (V) SPH_CK(cudaMemcpyAsync(V, hv.p + off, sizeof(T2<T>) * N_, cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+    }
+    Snap<T> &slot(int k)
+    {
+        if (!slots[k]) slots[k].reset(new Snap<T>());
+        return *slots[k];
+    }
+    void bind(const Sys<T> &s)
+    {
+        if (s.N_ != N_) throw Error(ERR_ARG, "tape and state particle counts differ");
+        if (nsnap_ && recomp && !recomp->same_config(s))
+            throw Error(ERR_ARG, "checkpoint tape was bound to a state with another configuration");
+        if (nsnap_ && !recomp)
+            recomp.reset(new Sys<T>(s.prm, s.N_, nullptr, nullptr, s.opts));
+    }
+};
+
+// simulate! (src/driver.jl:92-115)
+template <typename T>
+void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tape)
+{
+    Field<T> *th = field_of(theta);
+    const Params &q = p ? *p : prm;
+    check_params(q);
+    check_shape(q, th);
+    const Phys<T> ph = make_phys<T>(q);
+    Tape<T> *tp = nullptr;
+    if (tape) {
+        tp = dynamic_cast<Tape<T> *>(tape);
+        if (!tp) throw Error(ERR_DTYPE, "tape has a different precision than the state");
+        if (tp->n_ + nsteps > tp->cap_)
+            throw Error(ERR_CAPACITY, "tape capacity " + std::to_string(tp->cap_) + " < " +
+                                          std::to_string(tp->n_ + nsteps) + " steps needed");
+        tp->bind(*this);
+    }
+    for (int64_t s = 0; s < nsteps; ++s) {
+        T2<T> *tx = nullptr, *tv = nullptr;
+        if (tp) {
+            const int64_t n = tp->n_;
+            if (tp->nsnap_ == 0) {
+                tx = tp->hx.p + (size_t)n * N_;
+                tv = tp->hv.p + (size_t)n * N_;
+            } else {
+                for (size_t k = 0; k < tp->descent.size(); ++k)
+                    if (tp->descent[k] == n) {
+                        save(tp->slot((int)k));
+                        tp->slotPos[k] = n;
+                    }
+            }
+            tp->n_ += 1;
+        }
+        step_impl(th->th.p, ph, tx, tv);
+    }
+    SPH_CK(cudaStreamSynchronize(rt_stream()));
+    rt_check_launch("simulate");
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint workspace + backward!
+// ---------------------------------------------------------------------------
+template <typename T> class Work final : public WorkI {
+  public:
+    int64_t N_;
+    int ngx, ngy;
+    DevBuf<T2<T>> gX[2], gV[2];
+    int gcur = 0;
+    DevBuf<T2<T>> abar, gXs, stage2;
+    DevBuf<T> galpha, grho;
+    DevBuf<unsigned long long> thetaAcc;
+    DevBuf<int> emax;
+    DevBuf<double> gtheta;
+    DevBuf<T> gthetaT;
+    DevBuf<T2<T>> outX, outV; // results in particle-id order
+    std::unique_ptr<Sys<T>> own;
+    bool haveResult = false;
+
+    Work(int64_t N, const Params &p) : N_(N), ngx(p.ngx), ngy(p.ngy)
+    {
+        check_params(p);
+        const size_t n1 = (size_t)std::max<int64_t>(N, 1);
+        for (int k = 0; k < 2; ++k) {
+            gX[k].alloc(n1);
+            gV[k].alloc(n1);
+            gX[k].zero();
+            gV[k].zero();
+        }
+        abar.alloc(n1); gXs.alloc(n1); stage2.alloc(n1); outX.alloc(n1); outV.alloc(n1);
+        galpha.alloc(n1); grho.alloc(n1);
+        thetaAcc.alloc(2 * (size_t)ngx * ngy);
+        emax.alloc(2);
+        gtheta.alloc((size_t)ngx * ngy);
+        gthetaT.alloc((size_t)ngx * ngy);
+        gtheta.zero();
+    }
+    int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
+    int64_t N() const override { return N_; }
+
+    // One reverse step at the pre-state held in (sx, sv); srcInv maps particle
+    // ids into the source's slots when the source is a recomputed state.
+    void reverse_step(Sys<T> &S, const T *theta, const Phys<T> &p, const T2<T> *sx,
+                      const T2<T> *sv, const int32_t *srcInv, int parity)
+    {
+        SPH_LAUNCH(K_GATHER, k_gather_state<T>, N_, N_, S.perm.p, srcInv, sx, sv, S.pos[S.cur].p,
+                   S.vel[S.cur].p);
+        bool did = false;
+        const int g2 = 1 - gcur;
+        S.maybe_rebuild(gX[gcur].p, gX[g2].p, gV[gcur].p, gV[g2].p, &did);
+        if (did) gcur = g2;
+        const NLView<T> v = S.view();
+        const T2<T> *vel = S.vel[S.cur].p;
+        SPH_LAUNCH(K_DENSITY, k_density_eos<T>, N_, v, p, (T *)nullptr, S.prho.p);
+        SPH_LAUNCH(K_ACCEL_DRAG, k_accel_drag_adj<T>, N_, v, p, vel, S.prho.p, theta, gX[gcur].p,
+                   gV[gcur].p, abar.p, galpha.p, emax.p + parity);
+        SPH_LAUNCH(K_PASS1, k_pass1_design<T>, N_, v, p, vel, S.prho.p, theta, abar.p, galpha.p,
+                   gXs.p, grho.p, gV[gcur].p);
+        SPH_LAUNCH(K_PASS2, k_pass2_axpy<T>, N_, v, p, grho.p, gXs.p, gX[gcur].p, galpha.p,
+                   emax.p + parity, thetaAcc.p);
+        const int64_t nn = (int64_t)ngx * ngy;
+        SPH_LAUNCH(K_THETA_NODE, k_theta_node, nn, nn, N_, thetaAcc.p, emax.p + parity,
+                   emax.p + (1 - parity), gtheta.p);
+    }
+
+    void backward(TapeI *tape, FieldI *theta, const Params *p, const void *seedX,
+                  const void *seedV, StateI *scratch, NLOpts opts, uint32_t *flagsOut) override;
+
+    void get(void *gXo, void *gVo, void *gth) override
+    {
+        if (!haveResult) throw Error(ERR_STATE, "no backward pass has run on this workspace");
+        if (N_ && gXo) SPH_CK(cudaMemcpyAsync(gXo, outX.p, outX.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+        if (N_ && gVo) SPH_CK(cudaMemcpyAsync(gVo, outV.p, outV.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+        if (gth) {
+            const int64_t nn = (int64_t)ngx * ngy;
+            SPH_LAUNCH(K_MISC, k_to_T<T>, nn, nn, gtheta.p, gthetaT.p);
+            SPH_CK(cudaMemcpyAsync(gth, gthetaT.p, gthetaT.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
+    }
+};
+
+template <typename T>
+void Work<T>::backward(TapeI *tape, FieldI *theta, const Params *pp, const void *seedX,
+                       const void *seedV, StateI *scratch, NLOpts opts, uint32_t *flagsOut)
+{
+    auto *tp = dynamic_cast<Tape<T> *>(tape);
+    if (!tp) throw Error(ERR_DTYPE, "tape has a different precision than the workspace");
+    if (tp->N_ != N_) throw Error(ERR_ARG, "tape and workspace particle counts differ");
+    auto *th = dynamic_cast<Field<T> *>(theta);
+    if (!th) throw Error(ERR_DTYPE, "theta has a different precision than the workspace");
+    if (th->nx_ != ngx || th->ny_ != ngy) throw Error(ERR_ARG, "theta shape does not match the workspace");
+    if (!pp) throw Error(ERR_ARG, "backward needs the parameters");
+    check_params(*pp);
+    if (pp->ngx != ngx || pp->ngy != ngy)
+        throw Error(ERR_ARG, "params (ngx, ngy) do not match the workspace");
+    const Phys<T> p = make_phys<T>(*pp);
+
+    // scratch State (src/driver.jl:153-156): fresh unless the caller passes one
+    Sys<T> *S = nullptr;
+    if (scratch) {
+        S = dynamic_cast<Sys<T> *>(scratch);
+        if (!S) throw Error(ERR_DTYPE, "scratch state has a different precision");
+        if (S->N_ != N_) throw Error(ERR_ARG, "scratch state particle count differs");
+    } else {
+        if (!own || own->opts.skin != opts.skin || own->opts.interval != opts.interval ||
+            own->opts.maxnb != opts.maxnb || own->prm.h != pp->h || own->prm.Lx != pp->Lx ||
+            own->prm.Ly != pp->Ly)
+            own.reset(new Sys<T>(*pp, N_, nullptr, nullptr, opts));
+        S = own.get();
+        // a fresh State: neighbour list never built, no flags
+        S->age = INT64_MAX;
+        S->flags.zero();
+    }
+
+    // seeds: copyto!(gX, seedX), copyto!(gV, seedV), id order -> S's cell order
+    gcur = 0;
+    if (N_) {
+        if (seedX) {
+            SPH_CK(cudaMemcpyAsync(stage2.p, seedX, stage2.bytes(), cudaMemcpyHostToDevice, rt_stream()));
+            SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, S->perm.p, stage2.p, gX[0].p);
+        } else {
+            gX[0].zero();
+        }
+        if (seedV) {
+            SPH_CK(cudaMemcpyAsync(stage2.p, seedV, stage2.bytes(), cudaMemcpyHostToDevice, rt_stream()));
+            SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, S->perm.p, stage2.p, gV[0].p);
+        } else {
+            gV[0].zero();
+        }
+    }
+    gtheta.zero();
+    thetaAcc.zero();
+    {
+        const int init[2] = {INT_MIN, INT_MIN};
+        SPH_CK(cudaMemcpyAsync(emax.p, init, sizeof(init), cudaMemcpyHostToDevice, rt_stream()));
+    }
+
+    const int64_t L = tp->n_;
+    int64_t rstep = 0; // reverse steps done (parity of the exponent slot)
+    tp->fwdSteps = 0;
+    if (tp->nsnap_ == 0) {
+        for (int64_t n = L - 1; n >= 0; --n) {
+            reverse_step(*S, th->th.p, p, tp->hx.p + (size_t)n * N_, tp->hv.p + (size_t)n * N_,
+                         nullptr, (int)(rstep & 1));
+            ++rstep;
+        }
+    } else if (L > 0) {
+        Sys<T> &R = *tp->recomp;
+        // snapshots taken by simulate!, in position order
+        std::vector<std::pair<int64_t, int>> taken;
+        for (size_t k = 0; k < tp->slotPos.size(); ++k)
+            if (tp->slotPos[k] >= 0 && tp->slotPos[k] < L) taken.push_back({tp->slotPos[k], (int)k});
+        std::sort(taken.begin(), taken.end());
+        if (taken.empty() || taken[0].first != 0)
+            throw Error(ERR_STATE, "checkpoint tape holds no snapshot of its first step");
+        const int C = tp->nsnap_;
+        // free slots: those not holding a descent snapshot (as a stack)
+        std::vector<int> freeSlots;
+        for (int k = C - 1; k >= 0; --k)
+            if (tp->slotPos[k] < 0 || tp->slotPos[k] >= L) freeSlots.push_back(k);
+        auto advance = [&](int64_t m) {
+            for (int64_t s = 0; s < m; ++s) R.step_impl(th->th.p, p, nullptr, nullptr);
+            tp->fwdSteps += m;
+        };
+        auto rev_at_R = [&](int64_t n) {
+            (void)n;
+            reverse_step(*S, th->th.p, p, R.pos[R.cur].p, R.vel[R.cur].p, R.invperm.p,
+                         (int)(rstep & 1));
+            ++rstep;
+        };
+        // reverse steps [a, b) with the state at a in `slot`, c slots available
+        // (including `slot`); recursion splits at plan_split.
+        std::function<void(int64_t, int64_t, int, int64_t)> seg =
+            [&](int64_t a, int64_t b, int slot, int64_t c) {
+                if (b - a == 1) {
+                    R.restore(tp->slot(slot));
+                    rev_at_R(a);
+                    return;
+                }
+                if (c <= 1 || freeSlots.empty()) {
+                    for (int64_t i = b - 1; i >= a; --i) {
+                        R.restore(tp->slot(slot));
+                        advance(i - a);
+                        rev_at_R(i);
+                    }
+                    return;
+                }
+                const int64_t m = plan_split(b - a, c);
+                R.restore(tp->slot(slot));
+                advance(m);
+                const int ns = freeSlots.back();
+                freeSlots.pop_back();
+                R.save(tp->slot(ns));
+                seg(a + m, b, ns, c - 1);
+                freeSlots.push_back(ns);
+                seg(a, a + m, slot, c);
+            };
+        const int K = (int)taken.size();
+        for (int k = K - 1; k >= 0; --k) {
+            const int64_t a = taken[k].first;
+            const int64_t b = (k == K - 1) ? L : taken[k + 1].first;
+            seg(a, b, taken[k].second, (int64_t)freeSlots.size() + 1);
+            freeSlots.push_back(taken[k].second);
+        }
+    }
+    SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gX[gcur].p, outX.p);
+    SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gV[gcur].p, outV.p);
+    haveResult = true;
+    SPH_CK(cudaStreamSynchronize(rt_stream()));
+    rt_check_launch("backward");
+    uint32_t f = S->take_flags();
+    if (flagsOut) *flagsOut = f;
+}
+
+} // namespace sphgb

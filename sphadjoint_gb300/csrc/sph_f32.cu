@@ -1,0 +1,15 @@
+// FP32 instantiation of the engine: same kernels, multiply-add contraction on
+// (checked against the FP64 oracle within a relative tolerance).
+#include "sph_engine.cuh"
+
+namespace sphgb {
+
+FieldI *make_field_f32(int ngx, int ngy, const void *host) { return new Field<float>(ngx, ngy, host); }
+TapeI *make_tape_f32(int64_t N, int64_t cap, int32_t nsnap) { return new Tape<float>(N, cap, nsnap); }
+StateI *make_state_f32(const Params &p, int64_t N, const void *X0, const void *V0, NLOpts o)
+{
+    return new Sys<float>(p, N, X0, V0, o);
+}
+WorkI *make_work_f32(int64_t N, const Params &p) { return new Work<float>(N, p); }
+
+} // namespace sphgb

@@ -1,0 +1,147 @@
+// Precision-independent interfaces between the C ABI (sph_capi.cu) and the
+// two precision instantiations of the engine (sph_f32.cu, sph_f64.cu), plus the
+// small runtime shared by both (stream, launch counter, kernel timers).
+#pragma once
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace sphgb {
+
+// SPHParams (src/params.jl:58-72); fields are converted to T by the engine.
+struct Params {
+    double h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
+    int32_t ngx, ngy;
+};
+
+// NeighborList knobs (src/neighbors.jl:174-175).
+struct NLOpts {
+    double skin;
+    int32_t interval;
+    int32_t maxnb;
+};
+
+enum Dtype : int32_t { F64 = 0, F32 = 1 };
+
+// Error with a status code that the C ABI returns.
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+enum Status : int32_t {
+    OK = 0,
+    ERR_ARG = 1,      // ArgumentError in the reference
+    ERR_CAPACITY = 2, // tape capacity exceeded (ArgumentError in simulate!)
+    ERR_CUDA = 3,
+    ERR_DTYPE = 4,
+    ERR_NOMEM = 5,
+    ERR_STATE = 6,
+};
+
+void cuda_check(cudaError_t e, const char *what);
+#define SPH_CK(call) ::sphgb::cuda_check((call), #call)
+
+// ---- runtime ---------------------------------------------------------------
+enum KernelId : int32_t {
+    K_ASSIGN = 0,
+    K_SCAN,
+    K_BUCKET,
+    K_RANK,
+    K_NLBUILD,
+    K_DENSITY,
+    K_ACCEL_INTEGRATE,
+    K_TAPE,
+    K_GATHER,
+    K_ACCEL_DRAG,
+    K_PASS1,
+    K_PASS2,
+    K_THETA_NODE,
+    K_MISC,
+    K_COUNT
+};
+
+cudaStream_t rt_stream();
+void rt_set_stream(cudaStream_t s);
+void rt_before_launch(int kid);
+void rt_after_launch(int kid);
+void rt_check_launch(const char *name);
+
+class FieldI {
+  public:
+    virtual ~FieldI() {}
+    virtual int dtype() const = 0;
+    virtual int ngx() const = 0;
+    virtual int ngy() const = 0;
+    virtual void upload(const void *host_colmajor) = 0;
+    virtual void upload_device(const void *dev_colmajor) = 0;
+};
+
+class TapeI {
+  public:
+    virtual ~TapeI() {}
+    virtual int dtype() const = 0;
+    virtual int64_t N() const = 0;
+    virtual int64_t capacity() const = 0;
+    virtual int64_t length() const = 0;
+    virtual int32_t snapshots() const = 0; // 0: full history
+    virtual void reset() = 0;
+    virtual void get(int64_t n, void *X, void *V) = 0;
+    virtual int64_t forward_steps() const = 0; // steps recomputed by the last backward
+};
+
+class StateI {
+  public:
+    virtual ~StateI() {}
+    virtual int dtype() const = 0;
+    virtual int64_t N() const = 0;
+    virtual void set(const void *X, const void *V) = 0;
+    virtual void get(void *X, void *V) = 0;
+    virtual void fields(void *rho, void *pterm, void *invrho, void *a, void *alpha) = 0;
+    virtual void keep_accel(bool on) = 0;
+    virtual void step(FieldI *theta, const Params *p) = 0;
+    virtual void simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tape) = 0;
+    virtual void build_cells() = 0;
+    virtual void build_neighbors() = 0;
+    virtual void celllist(int32_t *counts, int32_t *starts, int32_t *order) = 0;
+    virtual void neighbors(int32_t *indices, int32_t *nbcount) = 0;
+    virtual uint32_t take_flags() = 0;
+    virtual void grid(int32_t *nx, int32_t *ny, double *cs, int64_t *age) const = 0;
+    virtual void sync() = 0;
+};
+
+class WorkI {
+  public:
+    virtual ~WorkI() {}
+    virtual int dtype() const = 0;
+    virtual int64_t N() const = 0;
+    virtual void backward(TapeI *tape, FieldI *theta, const Params *p, const void *seedX,
+                          const void *seedV, StateI *scratch, NLOpts opts,
+                          uint32_t *flags) = 0;
+    virtual void get(void *gX, void *gV, void *gtheta) = 0;
+};
+
+#define SPH_DECLARE_FACTORIES(SFX)                                                           \
+    FieldI *make_field##SFX(int ngx, int ngy, const void *host);                             \
+    TapeI *make_tape##SFX(int64_t N, int64_t cap, int32_t nsnap);                            \
+    StateI *make_state##SFX(const Params &p, int64_t N, const void *X0, const void *V0,      \
+                            NLOpts o);                                                       \
+    WorkI *make_work##SFX(int64_t N, const Params &p);
+
+SPH_DECLARE_FACTORIES(_f32)
+SPH_DECLARE_FACTORIES(_f64)
+
+// ---- binomial checkpoint schedule (checkpoint_plan.cpp) ---------------------
+// Minimal number of forward steps needed to reverse l steps when the state at
+// the start of the range is held in one of c snapshot slots.
+int64_t plan_cost(int64_t l, int64_t c);
+// The split m in [1, l-1] that attains plan_cost (smallest such m).
+int64_t plan_split(int64_t l, int64_t c);
+// Snapshot positions taken while sweeping forward over l steps with c slots.
+std::vector<int64_t> plan_descent(int64_t l, int64_t c);
+
+} // namespace sphgb

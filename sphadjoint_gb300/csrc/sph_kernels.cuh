@@ -1,0 +1,643 @@
+// sm_103a kernels of the forward + adjoint WCSPH step (one template, two
+// instantiations: double with --fmad=false for reference-exact parity, float
+// with contraction for throughput).
+//
+// Data layout in HBM (all arrays in *cell order* = the sorted order of the last
+// rebuild, so every neighbour row is a contiguous slot range):
+//   pos, vel, xref, abar, gX, gV, gXs : T2 per particle (8 B FP32 / 16 B FP64)
+//   rho, galpha, grho                 : T per particle
+//   prho                              : T2 {p/rho^2, 1/rho} per particle
+//   perm / invperm                    : int32 slot -> particle id / id -> slot
+//   center                            : uint32 per particle (cx | cy<<16 | spill<<31)
+//   masks                             : 3 x uint64 per particle, row-major by row
+//   cellStart                         : int32 x (ncell + 1)
+// Reference kernels restated: src/neighbors.jl:44-80,192-245 (cell list and
+// neighbour list), src/forward.jl:25-147, src/adjoint.jl:30-228.
+#pragma once
+
+#include "sph_common.cuh"
+
+namespace sphgb {
+
+constexpr int kBlock = 256;
+
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+
+// ---------------------------------------------------------------------------
+// Exclusive scan (reduce-then-scan, three launches, no inter-block waits)
+// ---------------------------------------------------------------------------
+constexpr int kScanTile = 2048; // 256 threads x 8 items
+
+__device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *smem_warp, int32_t &total)
+{
+    const unsigned lane = lane_id(), warp = threadIdx.x >> 5;
+    int32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (unsigned)o) x += y;
+    }
+    if (lane == 31) smem_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        int32_t w = lane < (unsigned)nw ? smem_warp[lane] : 0;
+        int32_t s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= (unsigned)o) s += y;
+        }
+        if (lane < (unsigned)nw) smem_warp[lane] = s - w;
+        if (lane == (unsigned)nw - 1) smem_warp[32] = s;
+    }
+    __syncthreads();
+    total = smem_warp[32];
+    const int32_t r = x - v + smem_warp[warp];
+    __syncthreads();
+    return r;
+}
+
+static __global__ void k_scan_reduce(const int32_t *__restrict__ in, int64_t n, int32_t *__restrict__ bsum)
+{
+    __shared__ int32_t sw[33];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanTile / kBlock; ++k) {
+        const int64_t i = base + (int64_t)k * kBlock + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    int32_t tot;
+    block_excl_scan(s, sw, tot);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+
+// single block: exclusive scan of nb block sums in place
+static __global__ void k_scan_top(int32_t *__restrict__ bsum, int64_t nb)
+{
+    __shared__ int32_t sw[33];
+    int32_t carry = 0;
+    for (int64_t base = 0; base < nb; base += blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const int32_t v = i < nb ? bsum[i] : 0;
+        int32_t tot;
+        const int32_t e = block_excl_scan(v, sw, tot);
+        if (i < nb) bsum[i] = e + carry;
+        carry += tot;
+    }
+}
+
+// out[i] = exclusive prefix; out[n] = total; out2 (optional) = copy of out[0..n)
+static __global__ void k_scan_down(const int32_t *__restrict__ in, int64_t n,
+                            const int32_t *__restrict__ bsum, int32_t *__restrict__ out,
+                            int32_t *__restrict__ out2)
+{
+    __shared__ int32_t sw[33];
+    constexpr int IPT = kScanTile / kBlock;
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * IPT;
+    int32_t v[IPT];
+    int32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int64_t i = base + k;
+        v[k] = i < n ? in[i] : 0;
+        s += v[k];
+    }
+    int32_t tot;
+    int32_t run = block_excl_scan(s, sw, tot) + (bsum ? bsum[blockIdx.x] : 0);
+#pragma unroll
+    for (int k = 0; k < IPT; ++k) {
+        const int64_t i = base + k;
+        if (i < n) {
+            out[i] = run;
+            if (out2) out2[i] = run;
+        }
+        run += v[k];
+        if (i == n - 1) out[n] = run;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Cell list: _cl_assign! / cumsum! / _cl_fill! / _cl_sort_cells!
+// (src/neighbors.jl:44-114), fused with the permutation of particle data into
+// the new cell order.
+// ---------------------------------------------------------------------------
+
+// Cell of every particle (division form x / cs as in cell_index), warp-
+// aggregated histogram, and the displacement check of _nl_build!
+// (src/neighbors.jl:207-213) against the previous rebuild positions.
+template <typename T>
+__global__ void k_assign(int64_t N, const T2<T> *__restrict__ pos, const T2<T> *__restrict__ xref,
+                         int check, T dmax2, T cs, int nx, int ny, int32_t *__restrict__ cellTmp,
+                         int32_t *__restrict__ counts, uint32_t *__restrict__ flags)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < N;
+    int32_t c = -1;
+    if (live) {
+        const T2<T> x = pos[i];
+        if (check) {
+            const T2<T> xr = xref[i];
+            const T d2 = r2_exact<T>(sub_rn(x.x, xr.x), sub_rn(x.y, xr.y));
+            if (d2 > dmax2) atomicOr(flags, FLAG_DISPLACEMENT);
+        }
+        const int cx = cell_coord<T>(x.x / cs, nx);
+        const int cy = cell_coord<T>(x.y / cs, ny);
+        c = (cx - 1) + (cy - 1) * nx;
+        cellTmp[i] = c;
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, live);
+    if (live) {
+        const unsigned peers = __match_any_sync(act, c);
+        if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(counts + c, __popc(peers));
+    }
+}
+
+// Scatter every particle into its cell's bucket (arbitrary order inside the
+// bucket; the rank step below makes it deterministic).
+static __global__ void k_bucket(int64_t N, const int32_t *__restrict__ cellTmp,
+                         const int32_t *__restrict__ perm, int32_t *__restrict__ cursor,
+                         int32_t *__restrict__ bucketSrc, int32_t *__restrict__ bucketId)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < N;
+    const int32_t c = live ? cellTmp[i] : -1;
+    const unsigned act = __ballot_sync(0xffffffffu, live);
+    if (!live) return;
+    const unsigned peers = __match_any_sync(act, c);
+    const int leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if ((int)lane_id() == leader) base = atomicAdd(cursor + c, __popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const int32_t pos = base + __popc(peers & ((1u << lane_id()) - 1u));
+    bucketSrc[pos] = (int32_t)i;
+    bucketId[pos] = perm[i];
+}
+
+// _cl_sort_cells! as a rank: each particle counts the smaller ids in its cell
+// and moves its data straight to (cell start + rank) of the new order.
+template <typename T>
+__global__ void k_rank_permute(int64_t N, const int32_t *__restrict__ cellTmp,
+                               const int32_t *__restrict__ cellStart,
+                               const int32_t *__restrict__ bucketSrc,
+                               const int32_t *__restrict__ bucketId,
+                               const T2<T> *__restrict__ pos, const T2<T> *__restrict__ vel,
+                               T2<T> *__restrict__ posN, T2<T> *__restrict__ velN,
+                               T2<T> *__restrict__ xrefN, int32_t *__restrict__ permN,
+                               int32_t *__restrict__ invperm, const T2<T> *__restrict__ ex0,
+                               T2<T> *__restrict__ ex0N, const T2<T> *__restrict__ ex1,
+                               T2<T> *__restrict__ ex1N)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= N) return;
+    const int32_t src = bucketSrc[s];
+    const int32_t id = bucketId[s];
+    const int32_t c = cellTmp[src];
+    const int32_t b = cellStart[c], e = cellStart[c + 1];
+    int32_t rank = 0;
+    for (int32_t k = b; k < e; ++k) rank += (bucketId[k] < id) ? 1 : 0;
+    const int32_t dst = b + rank;
+    permN[dst] = id;
+    if (!posN) return; // cell list only (build! without a neighbour rebuild)
+    const T2<T> x = pos[src];
+    posN[dst] = x;
+    xrefN[dst] = x;
+    velN[dst] = vel[src];
+    invperm[id] = dst;
+    if (ex0) ex0N[dst] = ex0[src];
+    if (ex1) ex1N[dst] = ex1[src];
+}
+
+// _nl_build! (src/neighbors.jl:192-245): the scan centre uses x * invcs as
+// the reference does; a neighbour is kept if r2min < r^2 < rc^2, in scan order,
+// at most maxnb of them (overflow sets the flag, like flags[1]).
+template <typename T>
+__global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2, T r2min,
+                           const T2<T> *__restrict__ pos, const int32_t *__restrict__ cellStart,
+                           uint32_t *__restrict__ center, uint64_t *__restrict__ masks,
+                           int32_t *__restrict__ nbcount, uint32_t *__restrict__ flags)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const T2<T> xi = pos[i];
+    const int cx = cell_coord<T>(xi.x * invcs, nx);
+    const int cy = cell_coord<T>(xi.y * invcs, ny);
+    const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
+    const int jx1 = cx + 1 < nx ? cx + 1 : nx;
+    uint32_t spill = 0;
+    int m = 0;
+    bool over = false;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        uint64_t mk = 0;
+        const int jy = cy + r - 1;
+        if (jy >= 1 && jy <= ny) {
+            const int64_t row = (int64_t)(jy - 1) * nx;
+            const int64_t b = cellStart[row + jx0 - 1];
+            const int64_t e = cellStart[row + jx1];
+            if (e - b > 64) spill = 1;
+            for (int64_t j = b; j < e; ++j) {
+                const T2<T> xj = pos[j];
+                const T r2 = r2_exact<T>(sub_rn(xi.x, xj.x), sub_rn(xi.y, xj.y));
+                if (r2min < r2 && r2 < rc2) {
+                    if (m < maxnb) {
+                        if (j - b < 64) mk |= 1ull << (j - b);
+                        ++m;
+                    } else {
+                        over = true;
+                    }
+                }
+            }
+        }
+        masks[(int64_t)r * N + i] = mk;
+    }
+    center[i] = (uint32_t)cx | ((uint32_t)cy << 16) | (spill << 31);
+    nbcount[i] = m;
+    if (over) atomicOr(flags, FLAG_NL_OVERFLOW);
+}
+
+// ---------------------------------------------------------------------------
+// Forward: density_kernel! + eos_kernel! (fused), accel_kernel! +
+// integrate_kernel! (fused; positions and velocities double-buffered because
+// neighbours read the pre-step state).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_density_eos(NLView<T> v, Phys<T> p,
+                                                        T *__restrict__ rho,
+                                                        T2<T> *__restrict__ prho)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    const T2<T> xi = v.pos[i];
+    T acc = (T)0;
+    for_each_neighbor<T>(v, i, [&](int64_t j) {
+        const T2<T> xj = v.pos[j];
+        const T dx = xi.x - xj.x;
+        const T dy = xi.y - xj.y;
+        const T r2 = dx * dx + dy * dy;
+        if (r2 < p.r2max) {
+            const T q = sqrt(r2) * p.invh;
+            const T u = (T)1 - (T)0.5 * q;
+            const T u2 = u * u;
+            acc += p.m * (p.A * u2 * u2 * ((T)2 * q + (T)1));
+        }
+    });
+    const T ri = acc + p.m * p.A;
+    if (rho) rho[i] = ri;
+    const T inv = (T)1 / ri;
+    prho[i] = mk2<T>(p.c2 * (ri - p.rho0) * inv * inv, inv);
+}
+
+// Pressure + Morris viscosity + gravity + wall (accel_kernel!) and the semi-
+// implicit Euler update with implicit Brinkman drag (integrate_kernel!).
+template <typename T>
+__device__ __forceinline__ void accel_sum(const NLView<T> &v, const Phys<T> &p,
+                                          const T2<T> *__restrict__ vel,
+                                          const T2<T> *__restrict__ prho, int64_t i,
+                                          const T2<T> &xi, const T2<T> &vi, T &ax, T &ay)
+{
+    const T2<T> pi = prho[i];
+    const T pti = pi.x, iri = pi.y;
+    ax = (T)0;
+    ay = (T)0;
+    for_each_neighbor<T>(v, i, [&](int64_t j) {
+        const T2<T> xj = v.pos[j];
+        const T dx = xi.x - xj.x;
+        const T dy = xi.y - xj.y;
+        const T r2 = dx * dx + dy * dy;
+        if (r2 < p.r2max) {
+            const T q = sqrt(r2) * p.invh;
+            const T u = (T)1 - (T)0.5 * q;
+            const T F = p.Fc * u * u * u;
+            const T2<T> pj = prho[j];
+            const T Pij = p.m * (pti + pj.x);
+            ax -= Pij * F * dx;
+            ay -= Pij * F * dy;
+            const T C = p.twomumass * iri * pj.y * F;
+            const T2<T> vj = vel[j];
+            ax += C * (vi.x - vj.x);
+            ay += C * (vi.y - vj.y);
+        }
+    });
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_accel_integrate(NLView<T> v, Phys<T> p, const T2<T> *__restrict__ vel,
+                      const T2<T> *__restrict__ prho, const T *__restrict__ theta,
+                      T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
+                      T2<T> *__restrict__ aOut, T *__restrict__ alphaOut,
+                      uint32_t *__restrict__ flags)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    const T2<T> xi = v.pos[i];
+    const T2<T> vi = vel[i];
+    T ax, ay;
+    accel_sum<T>(v, p, vel, prho, i, xi, vi, ax, ay);
+    const T al = interp_alpha_value<T>(theta, xi.x, xi.y, p);
+    ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
+    ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
+    if (aOut) aOut[i] = mk2<T>(ax, ay);
+    if (alphaOut) alphaOut[i] = al;
+    const T D = (T)1 / ((T)1 + p.dt * al);
+    const T v1 = (vi.x + p.dt * ax) * D;
+    const T v2 = (vi.y + p.dt * ay) * D;
+    const T x1 = xi.x + p.dt * v1;
+    const T x2 = xi.y + p.dt * v2;
+    velOut[i] = mk2<T>(v1, v2);
+    posOut[i] = mk2<T>(x1, x2);
+    if (!(isfinite(x1) && isfinite(x2) && isfinite(v1) && isfinite(v2)))
+        atomicOr(flags, FLAG_NONFINITE);
+}
+
+// Tape slot in particle-id order (_tape_store!, src/driver.jl:73-77).
+template <typename T>
+__global__ void k_tape_store(int64_t N, const int32_t *__restrict__ perm,
+                             const T2<T> *__restrict__ pos, const T2<T> *__restrict__ vel,
+                             T2<T> *__restrict__ tx, T2<T> *__restrict__ tv)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const int32_t id = perm[i];
+    tx[id] = pos[i];
+    tv[id] = vel[i];
+}
+
+// _tape_load! into cell order: slot t takes particle perm[t]; when srcInv is
+// given the source is itself in cell order (a recomputed state) and the id is
+// mapped through its inverse permutation.
+template <typename T>
+__global__ void k_gather_state(int64_t N, const int32_t *__restrict__ perm,
+                               const int32_t *__restrict__ srcInv,
+                               const T2<T> *__restrict__ sx, const T2<T> *__restrict__ sv,
+                               T2<T> *__restrict__ pos, T2<T> *__restrict__ vel)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    int32_t s = perm[t];
+    if (srcInv) s = srcInv[s];
+    pos[t] = sx[s];
+    vel[t] = sv[s];
+}
+
+// id-ordered (interleaved) host layout <-> cell order
+template <typename T>
+__global__ void k_scatter_to_ids(int64_t N, const int32_t *__restrict__ perm,
+                                 const T2<T> *__restrict__ a, T2<T> *__restrict__ out)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    out[perm[t]] = a[t];
+}
+
+template <typename T>
+__global__ void k_scatter_to_ids1(int64_t N, const int32_t *__restrict__ perm,
+                                  const T *__restrict__ a, T *__restrict__ out)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    out[perm[t]] = a[t];
+}
+
+template <typename T>
+__global__ void k_gather_from_ids(int64_t N, const int32_t *__restrict__ perm,
+                                  const T2<T> *__restrict__ a, T2<T> *__restrict__ out)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= N) return;
+    out[t] = a[perm[t]];
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint (gather form, src/adjoint.jl)
+// ---------------------------------------------------------------------------
+
+// Accel recompute (accel_kernel!, for a_rest and alpha) + _adj_integrate!
+// (gV += dt gX) + _adj_drag! (implicit Brinkman VJP). Also records the
+// largest binary exponent of |galpha| for the exact theta reduction.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_accel_drag_adj(NLView<T> v, Phys<T> p, const T2<T> *__restrict__ vel,
+                     const T2<T> *__restrict__ prho, const T *__restrict__ theta,
+                     const T2<T> *__restrict__ gX, T2<T> *__restrict__ gV,
+                     T2<T> *__restrict__ abar, T *__restrict__ galpha,
+                     int *__restrict__ emax)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int e = INT_MIN;
+    if (i < v.N) {
+        const T2<T> xi = v.pos[i];
+        const T2<T> vi = vel[i];
+        T ax, ay;
+        accel_sum<T>(v, p, vel, prho, i, xi, vi, ax, ay);
+        const T al = interp_alpha_value<T>(theta, xi.x, xi.y, p);
+        ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
+        ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
+        const T2<T> gx = gX[i];
+        T2<T> gv = gV[i];
+        gv.x += p.dt * gx.x;
+        gv.y += p.dt * gx.y;
+        const T D = (T)1 / ((T)1 + p.dt * al);
+        const T vx = (vi.x + p.dt * ax) * D;
+        const T vy = (vi.y + p.dt * ay) * D;
+        abar[i] = mk2<T>(p.dt * D * gv.x, p.dt * D * gv.y);
+        const T ga = -p.dt * D * (vx * gv.x + vy * gv.y);
+        galpha[i] = ga;
+        gV[i] = mk2<T>(D * gv.x, D * gv.y);
+        if (ga != (T)0 && isfinite(ga)) e = ilogb((double)ga) + 1; // |ga| < 2^e
+    }
+    // block max, then one atomic per block
+    for (int o = 16; o > 0; o >>= 1) {
+        const int y = __shfl_xor_sync(0xffffffffu, e, o);
+        e = y > e ? y : e;
+    }
+    __shared__ int sm[kBlock / 32];
+    if (lane_id() == 0) sm[threadIdx.x >> 5] = e;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int b = sm[0];
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = sm[w] > b ? sm[w] : b;
+        if (b != INT_MIN) atomicMax(emax, b);
+    }
+}
+
+// adj_pass1_kernel! (src/adjoint.jl:30-122) + the per-particle half of
+// adj_design_kernel! (gXs += galpha * grad alpha, src/adjoint.jl:173-175)
+// + _axpy2!(gV, gVs).
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_pass1_design(NLView<T> v, Phys<T> p, const T2<T> *__restrict__ vel,
+                   const T2<T> *__restrict__ prho, const T *__restrict__ theta,
+                   const T2<T> *__restrict__ abar, const T *__restrict__ galpha,
+                   T2<T> *__restrict__ gXs, T *__restrict__ grho, T2<T> *__restrict__ gV)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    const T2<T> xi = v.pos[i];
+    const T2<T> vi = vel[i];
+    const T2<T> ab = abar[i];
+    const T2<T> pi = prho[i];
+    const T pti = pi.x, iri = pi.y;
+    T gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
+    for_each_neighbor<T>(v, i, [&](int64_t j) {
+        const T2<T> xj = v.pos[j];
+        const T dx = xi.x - xj.x;
+        const T dy = xi.y - xj.y;
+        const T r2 = dx * dx + dy * dy;
+        if (r2 < p.r2max) {
+            const T r = sqrt(r2);
+            const T q = r * p.invh;
+            const T u = (T)1 - (T)0.5 * q;
+            const T F = p.Fc * u * u * u;
+            const T G = p.Gc * u * u;
+            const T2<T> pj = prho[j];
+            const T Pij = p.m * (pti + pj.x);
+            const T Cbase = p.twomumass * iri * pj.y;
+            const T C = Cbase * F;
+            const T2<T> abj = abar[j];
+            const T2<T> vj = vel[j];
+            const T dax = ab.x - abj.x;
+            const T day = ab.y - abj.y;
+            const T dvx = vi.x - vj.x;
+            const T dvy = vi.y - vj.y;
+            const T ad_d = -(dax * dx + day * dy);
+            const T ad_v = dax * dvx + day * dvy;
+            gx -= Pij * F * dax;
+            gy -= Pij * F * day;
+            const T Fbar = Pij * ad_d + Cbase * ad_v;
+            const T w = Fbar * G * p.invh / r;
+            gx += w * dx;
+            gy += w * dy;
+            gvx += C * dax;
+            gvy += C * day;
+            grh -= C * ad_v * iri;
+            sumS += F * ad_d;
+        }
+    });
+    grh += ((T)(-2) * p.m * pti * iri) * sumS;
+    grh += p.c2 * p.m * iri * iri * sumS;
+    gx += ab.x * wall_daccel<T>(xi.x, p.Lx, p.kw);
+    gy += ab.y * wall_daccel<T>(xi.y, p.Ly, p.kw);
+    T al, dadx, dady;
+    interp_alpha<T>(theta, xi.x, xi.y, p, al, dadx, dady);
+    const T ga = galpha[i];
+    gXs[i] = mk2<T>(gx + ga * dadx, gy + ga * dady);
+    grho[i] = grh;
+    T2<T> g = gV[i];
+    g.x += gvx;
+    g.y += gvy;
+    gV[i] = g;
+}
+
+// 128-bit two's-complement fixed-point accumulation: integer addition is
+// associative, so the dJ/dtheta sums are exact and independent of the order in
+// which particles arrive. acc[0] = low word, acc[1] = high word.
+__device__ __forceinline__ void fixed_add(unsigned long long *acc, double c, int S)
+{
+    if (c == 0.0) return;
+    double a = rint(ldexp(fabs(c), S));
+    if (a == 0.0) return;
+    const double hid = floor(ldexp(a, -64));
+    const double lod = a - ldexp(hid, 64);
+    unsigned long long hi = (unsigned long long)hid;
+    unsigned long long lo = (unsigned long long)lod;
+    if (c < 0.0) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    const unsigned long long old = atomicAdd(acc, lo);
+    const unsigned long long h = hi + ((old + lo < old) ? 1ull : 0ull);
+    if (h) atomicAdd(acc + 1, h);
+}
+
+__host__ __device__ __forceinline__ int theta_scale(int emax, int64_t N)
+{
+    int lg = 0;
+    while (((int64_t)1 << lg) < N + 1 && lg < 62) ++lg;
+    return 124 - emax - lg;
+}
+
+// adj_pass2_kernel! (src/adjoint.jl:126-156) + _axpy2!(gX, gXs) + the theta
+// write-back of adj_design_kernel! (src/adjoint.jl:177-184), done as an exact
+// deterministic reduction keyed by design node instead of float atomics.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+    k_pass2_axpy(NLView<T> v, Phys<T> p, const T *__restrict__ grho,
+                 const T2<T> *__restrict__ gXs, T2<T> *__restrict__ gX,
+                 const T *__restrict__ galpha, const int *__restrict__ emax,
+                 unsigned long long *__restrict__ thetaAcc)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= v.N) return;
+    const T2<T> xi = v.pos[i];
+    const T gri = grho[i];
+    T gx = 0, gy = 0;
+    for_each_neighbor<T>(v, i, [&](int64_t j) {
+        const T2<T> xj = v.pos[j];
+        const T dx = xi.x - xj.x;
+        const T dy = xi.y - xj.y;
+        const T r2 = dx * dx + dy * dy;
+        if (r2 < p.r2max) {
+            const T q = sqrt(r2) * p.invh;
+            const T u = (T)1 - (T)0.5 * q;
+            const T w = p.m * (p.Fc * u * u * u) * (gri + grho[j]);
+            gx += w * dx;
+            gy += w * dy;
+        }
+    });
+    T2<T> gs = gXs[i];
+    gs.x += gx;
+    gs.y += gy;
+    T2<T> g = gX[i];
+    g.x += gs.x;
+    g.y += gs.y;
+    gX[i] = g;
+
+    const T ga = galpha[i];
+    const int em = *emax;
+    if (ga != (T)0 && em != INT_MIN) {
+        int i0, j0;
+        T fx, fy, ax, ay;
+        interp_cell<T>(xi.x, xi.y, p, i0, j0, fx, fy, ax, ay);
+        const int S = theta_scale(em, v.N);
+        const int64_t l00 = (int64_t)j0 + (int64_t)i0 * p.ngy;
+        fixed_add(thetaAcc + 2 * l00, (double)(ga * ((T)1 - fx) * ((T)1 - fy)), S);
+        fixed_add(thetaAcc + 2 * (l00 + p.ngy), (double)(ga * fx * ((T)1 - fy)), S);
+        fixed_add(thetaAcc + 2 * (l00 + 1), (double)(ga * ((T)1 - fx) * fy), S);
+        fixed_add(thetaAcc + 2 * (l00 + p.ngy + 1), (double)(ga * fx * fy), S);
+    }
+}
+
+// Per design node: gtheta += this step's exact sum; clear the accumulator and
+// the exponent slot the next step will use.
+static __global__ void k_theta_node(int64_t nnode, int64_t N, unsigned long long *__restrict__ acc,
+                             const int *__restrict__ emax, int *__restrict__ emaxNext,
+                             double *__restrict__ gtheta)
+{
+    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (n == 0) *emaxNext = INT_MIN;
+    if (n >= nnode) return;
+    unsigned long long lo = acc[2 * n], hi = acc[2 * n + 1];
+    if ((lo | hi) == 0ull) return;
+    acc[2 * n] = 0ull;
+    acc[2 * n + 1] = 0ull;
+    const bool neg = (long long)hi < 0;
+    if (neg) {
+        lo = ~lo + 1ull;
+        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    }
+    double vv = ldexp((double)hi, 64) + (double)lo;
+    if (neg) vv = -vv;
+    gtheta[n] += ldexp(vv, -theta_scale(*emax, N));
+}
+
+template <typename T>
+__global__ void k_to_T(int64_t n, const double *__restrict__ a, T *__restrict__ out)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (T)a[i];
+}
+
+} // namespace sphgb

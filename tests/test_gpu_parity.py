@@ -1,0 +1,178 @@
+"""CUDA library vs CPU oracle on the same seeded inputs, through the C ABI.
+
+FP64: cell lists and neighbour rows are compared exactly; positions,
+velocities, dJ/dX0 and dJ/dV0 bit for bit (same summation order, no FMA);
+dJ/dtheta within 1e-12 relative (the oracle sums it serially in particle
+order, the library with an exact fixed-point reduction).
+FP32: within 1e-5 relative of the FP64 oracle on short horizons.
+"""
+import numpy as np
+import pytest
+
+import cases as K
+from runners import linear_seeds, run_gpu, run_oracle
+
+pytestmark = pytest.mark.gpu
+
+S = pytest.importorskip("sphadjoint_gb300")
+import oracle as O  # noqa: E402
+
+
+def _states(case, dtype="f64", **kw):
+    p = S.SPHParams(**case["p"], dtype=dtype)
+    st = S.State(case["X0"], case["V0"], p, **kw)
+    o = O.Oracle(dtype)
+    ost = o.state(O.params(**case["p"]), case["X0"], case["V0"], **kw)
+    return p, st, o, ost
+
+
+@pytest.mark.parametrize("maker", [K.random_points_case, K.dambreak_case])
+def test_celllist_bit_exact(maker):
+    case = maker()
+    p, st, o, ost = _states(case)
+    S.build(st)
+    ost.build_cells()
+    g = st.celllist()
+    c = ost.cells()
+    assert np.array_equal(g["counts"], c["counts"])
+    assert np.array_equal(g["starts"], c["starts"])
+    assert np.array_equal(g["order"], c["order"])
+    # build_neighbors! gives the same cell list, and the same rows in order
+    S.build_neighbors(st)
+    ost.build_neighbors(case["p"]["h"])
+    g = st.celllist()
+    assert np.array_equal(g["order"], c["order"])
+    gi, gn = st.neighbors()
+    oi, on = ost.neighbors()
+    assert np.array_equal(gn, on)
+    for i in range(st.N):
+        assert np.array_equal(gi[i, : gn[i]], oi[i, : on[i]]), i
+    assert st.take_flags() == ost.take_flags() == 0
+
+
+def test_density_bit_exact():
+    case = K.random_points_case()
+    p, st, o, ost = _states(case)
+    S.build_neighbors(st)
+    ost.build_neighbors(case["p"]["h"])
+    ost.density(O.params(**case["p"]))
+    S.step(st, np.zeros((7, 9)), p)  # density is the first pass of a step
+    # the step rebuilt nothing (age 0 < interval) and computed rho at X0
+    g = st.fields()
+    r = ost.fields()
+    assert np.array_equal(g["rho"], r["rho"])
+    assert np.array_equal(g["pterm"], r["pterm"])
+    assert np.array_equal(g["invrho"], r["invrho"])
+
+
+@pytest.mark.parametrize("interval", [1, 4])
+def test_forward_bit_exact_dambreak(interval):
+    case = K.dambreak_case()
+    g = run_gpu(case, 300, interval=interval, tape=False)
+    r = run_oracle(case, 300, interval=interval, tape=False)
+    assert g["flags"] == r["flags"]
+    assert np.array_equal(g["X"], r["X"])
+    assert np.array_equal(g["V"], r["V"])
+
+
+@pytest.mark.parametrize("maker", [K.adjoint_case, K.gradcheck_case])
+def test_adjoint_bit_exact(maker):
+    case = maker()
+    seeds = linear_seeds(case)
+    g = run_gpu(case, case["nsteps"], seeds=seeds)
+    r = run_oracle(case, case["nsteps"], seeds=seeds)
+    assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["V"], r["V"])
+    assert np.array_equal(g["gX"], r["gX"])
+    assert np.array_equal(g["gV"], r["gV"])
+    assert K.relerr(g["gtheta"], r["gtheta"]) <= 1e-12
+    assert np.max(np.abs(r["gtheta"])) > 0
+
+
+def test_adjoint_dambreak_ke_interval4():
+    case = K.dambreak_case(theta_seed=3)
+    p = case["p"]
+    seeds = lambda X, V: K.ke_seeds(X, V, p)[1:]  # noqa: E731
+    n = 120
+    g = run_gpu(case, n, seeds=seeds)
+    r = run_oracle(case, n, seeds=seeds)
+    assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["V"], r["V"])
+    assert np.array_equal(g["gX"], r["gX"])
+    assert np.array_equal(g["gV"], r["gV"])
+    assert K.relerr(g["gtheta"], r["gtheta"]) <= 1e-12
+
+
+def test_checkpointed_tape_matches_full_tape():
+    case = K.adjoint_case(seed=5)
+    seeds = linear_seeds(case)
+    n = 40
+    full = run_gpu(case, n, seeds=seeds, interval=3)
+    for c in (1, 2, 3, 6):
+        ck = run_gpu(case, n, seeds=seeds, interval=3, snapshots=c)
+        assert np.array_equal(ck["gX"], full["gX"]), c
+        assert np.array_equal(ck["gV"], full["gV"]), c
+        assert np.array_equal(ck["gtheta"], full["gtheta"]), c
+        # backward recomputes everything the optimal schedule needs except the
+        # advances of its first descent, which simulate! already made
+        lib = S.load()
+        pos, left, slots = 0, n, c
+        while left > 1 and slots >= 2:
+            m = lib.sph_plan_split(left, slots)
+            pos, left, slots = pos + m, left - m, slots - 1
+        assert ck["tape"].recomputed_steps() == lib.sph_plan_cost(n, c) - pos, c
+
+
+def test_fp32_close_to_fp64_oracle():
+    case = K.adjoint_case(seed=2)
+    seeds = linear_seeds(case)
+    g = run_gpu(case, case["nsteps"], dtype="f32", seeds=seeds)
+    r = run_oracle(case, case["nsteps"], seeds=seeds)
+    assert K.relerr(g["X"], r["X"]) <= 1e-5
+    assert K.relerr(g["V"], r["V"]) <= 1e-5
+    assert K.relerr(g["gX"], r["gX"]) <= 1e-5
+    assert K.relerr(g["gV"], r["gV"]) <= 1e-5
+    assert K.relerr(g["gtheta"], r["gtheta"]) <= 1e-5
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_repeat_runs_bit_identical(dtype):
+    case = K.dambreak_case(theta_seed=4, jitter=0.05)
+    p = case["p"]
+    seeds = lambda X, V: K.ke_seeds(X, V, p)[1:]  # noqa: E731
+    a = run_gpu(case, 80, dtype=dtype, seeds=seeds)
+    b = run_gpu(case, 80, dtype=dtype, seeds=seeds)
+    for k in ("X", "V", "gX", "gV", "gtheta"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_dense_cells_spill_and_overflow_match_oracle():
+    # h = 3 dp: ~160 neighbours within the skin radius, rows of ~150 slots
+    # (beyond the 64-slot masks) and maxnb = 64 truncation, like the reference.
+    rng = np.random.default_rng(9)
+    dp = 0.02
+    p = dict(h=3 * dp, m=dp ** 2, rho0=1.0, c=10.0, mu=0.02, dt=1e-4, Lx=1.0, Ly=0.6,
+             kw=1e4, ngx=9, ngy=7)
+    X0 = K.lattice_block(14, 12, dp, dp, dp, 0.1 * dp, rng)
+    case = dict(p=p, X0=X0, V0=0.05 * rng.standard_normal(X0.shape), theta=np.ones((7, 9)),
+                cX=rng.standard_normal(X0.shape), cV=rng.standard_normal(X0.shape))
+    seeds = linear_seeds(case)
+    g = run_gpu(case, 10, seeds=seeds, interval=2)
+    r = run_oracle(case, 10, seeds=seeds, interval=2)
+    assert r["flags"] & 1 and g["flags"] == r["flags"]
+    assert g["bflags"] == r["bflags"]
+    assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["V"], r["V"])
+    assert np.array_equal(g["gX"], r["gX"]) and np.array_equal(g["gV"], r["gV"])
+    assert K.relerr(g["gtheta"], r["gtheta"]) <= 1e-12
+
+
+def test_particles_outside_tank_and_single_particle():
+    case = K.adjoint_case(seed=3)
+    case["X0"][:, :3] = [[-0.05, 1.07, 0.5], [0.5, -0.02, 1.1]]  # beyond the walls
+    seeds = linear_seeds(case)
+    g = run_gpu(case, 8, seeds=seeds)
+    r = run_oracle(case, 8, seeds=seeds)
+    assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["gX"], r["gX"])
+    one = dict(p=case["p"], X0=np.array([[0.5], [0.5]]), V0=np.array([[0.1], [0.0]]),
+               theta=case["theta"], cX=np.ones((2, 1)), cV=np.ones((2, 1)))
+    g = run_gpu(one, 5, seeds=linear_seeds(one))
+    r = run_oracle(one, 5, seeds=linear_seeds(one))
+    assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["gV"], r["gV"])
