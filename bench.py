@@ -1,0 +1,388 @@
+#!/usr/bin/env python
+"""Forward + adjoint WCSPH throughput on one GB300.
+
+Workload ("single large instance"): a 1024 x 1024 jittered lattice (1,048,576
+particles, dx = 1e-3, uniform jitter +-0.05 dx, seed 1) at the left of a
+2.048 x 1.28 tank; h = 1.3 dx, rho0 = 1000, m = rho0 dx^2, c0 = 10 sqrt(2 g H),
+mu = 0.02, kw = 5e4, dt = 0.25 h / c0; theta 256 x 256, seeded uniform [0,1]
+smoothed by a 5 x 5 box filter (seed 2); 1000 steps in FP32 with a binomial
+checkpoint tape of 32 snapshots; objective = kinetic energy of the right half.
+A bench step is one complete solve (forward sweep, objective, reverse sweep
+with recomputation). Metric: forward+adjoint particle-steps/s
+(N x time steps / solve time). Synthetic data; no dataset is involved.
+
+value: device-resident inputs (the initial state is cloned on the device),
+timed with CUDA events on the library stream. e2e: the same solve through
+the C ABI with host buffers (State from host X0, Array(X_T), host objective,
+host seeds, Array(gradients)), wall-clock with the copies inside.
+--impl reference: the CPU restatement of the reference (the Julia reference
+cannot run here) on all host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# algorithmic HBM bytes per particle per launch (compulsory traffic of the
+# minimal dataflow, s = sizeof(T)): read/write sets of each fused pass
+ALGO_WORDS = {
+    "density": 4,          # read X (2) -> write p/rho^2, 1/rho (2)
+    "accel_integrate": 10, # read X, V, pterm, invrho (6) -> write X', V' (4)
+    "accel_drag": 15,      # read X, V, pterm, invrho, gX, gV (10) -> abar, galpha, gV (5)
+    "pass1": 16,           # read abar, X, V, pterm, invrho, galpha, gV (11) -> gV, gXs, grho (5)
+    "pass2": 9,            # read grho, X, gXs, gX (7) -> gX (2)
+}
+
+
+def workload(n_side=1024, nsteps=1000, snapshots=32, ntheta=256, dtype="f32"):
+    dx = 1e-3
+    H = n_side * dx
+    h = 1.3 * dx
+    c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+    p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0,
+             Lx=2.0 * H, Ly=1.25 * H, kw=5e4, ngx=ntheta, ngy=ntheta)
+    rng = np.random.default_rng(1)
+    xs = dx + dx * np.arange(n_side)
+    X, Y = np.meshgrid(xs, xs)
+    X0 = np.vstack([X.ravel(), Y.ravel()]) + rng.uniform(-0.05 * dx, 0.05 * dx, (2, n_side ** 2))
+    V0 = np.zeros_like(X0)
+    t = np.random.default_rng(2).random((ntheta, ntheta))
+    pad = np.pad(t, 2, mode="edge")
+    theta = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
+    cfg = {"workload": f"single large instance: {n_side}x{n_side} jittered lattice "
+                       f"({n_side * n_side} particles), {nsteps} steps {dtype.upper()}, "
+                       f"binomial checkpointing with {snapshots} snapshots, theta {ntheta}x{ntheta}",
+           "particles": n_side * n_side, "time_steps": nsteps, "snapshots": snapshots,
+           "theta": [ntheta, ntheta], "tank": [p["Lx"], p["Ly"]], "dx": dx,
+           "skin": 0.2, "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half",
+           "l2": "inputs larger than L2 (checkpoint set and per-step arrays stream >1 GB per solve)"}
+    return p, X0, V0, theta, cfg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ["clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device=0):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == len(self.FIELDS):
+                self.rows.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if not self.rows:
+            return None
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if r[4 + k].lower() in ("active", "0x1", "1")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64):
+    """Time the oracle (forward + adjoint with a full tape) on all host cores
+    on the first few time steps of the workload; returns particle-steps/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    o = O.Oracle(dtype)
+    op = O.params(**p)
+    th = o.theta(theta)
+    N = X0.shape[1]
+
+    def run(nsteps):
+        st = o.state(op, X0, V0)
+        tp = o.tape(N, nsteps)
+        t0 = time.perf_counter()
+        o.simulate(st, th, op, nsteps, tp)
+        X, V = st.get()
+        right = X[:, 0] > p["Lx"] / 2
+        sV = np.where(right[:, None], p["m"] * V, 0.0)
+        ws = o.workspace(N, op)
+        o.backward(ws, tp, th, op, np.zeros_like(X), sV)
+        return time.perf_counter() - t0
+
+    t1 = run(1)
+    n = int(max(1, min(max_steps, budget_s / max(t1, 1e-3))))
+    t = run(n) if n > 1 else t1
+    return {"value": N * n / t, "unit": "particle-steps/s", "cores": O.get_threads(),
+            "kind": "port",
+            "sample": f"{N} particles x {n} time steps, forward + adjoint with a full tape, "
+                      f"{dtype.upper()}, C restatement of the reference with OpenMP",
+            "seconds": t}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    p, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
+                                     args.dtype)
+    if rank != 0:
+        return
+    budget = args.ref_step_seconds
+    for _ in range(args.warmup):
+        cpu_sample(p, X0, V0, theta, args.dtype, budget_s=budget / 4, max_steps=2)
+    tot_ps, tot_t = 0.0, 0.0
+    last = None
+    for _ in range(args.steps):
+        last = cpu_sample(p, X0, V0, theta, args.dtype, budget_s=budget)
+        tot_ps += last["value"] * last["seconds"]
+        tot_t += last["seconds"]
+    v = tot_ps / tot_t
+    line = {"impl": "reference", "metric": "fwd+adjoint particle-steps/s", "value": v,
+            "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.dtype, "data": "synthetic", "config": cfg,
+            "cpu_baseline": {k: last[k] for k in ("unit", "cores", "kind", "sample")} | {"value": v},
+            "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "the reference is Julia (KernelAbstractions); Julia is not installed, so its "
+                    "CPU path is timed through the C restatement in oracle/"}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    world, rank, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import sphadjoint_gb300 as S
+    from sphadjoint_gb300 import _lib as LB
+
+    L = S.load()
+    stream = torch.cuda.Stream()
+    LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
+
+    p_d, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
+                                       args.dtype)
+    p = S.SPHParams(**p_d, dtype=args.dtype)
+    N = X0.shape[1]
+    pc = p.c_struct()
+    st0 = S.State(X0, V0, p)             # pristine initial state (device)
+    st = S.State(X0, V0, p)
+    th = S.DesignField(theta, args.dtype)
+    tape = S.Tape(N, args.nsteps, p, snapshots=args.snapshots)
+    ws = S.AdjointWorkspace(N, p)
+    flags = C.c_uint32()
+    J = C.c_double()
+
+    def solve():
+        LB.check(L.sph_state_assign(st.h, st0.h))
+        tape.reset()
+        LB.check(L.sph_simulate(st.h, th.h, C.byref(pc), args.nsteps, tape.h, C.byref(flags)))
+        LB.check(L.sph_objective(ws.h, st.h, 0, None, C.byref(pc), C.byref(J)))
+        LB.check(L.sph_backward_seeded(ws.h, tape.h, th.h, C.byref(pc), None, 0.2, 4, 64,
+                                       C.byref(flags)))
+
+    for _ in range(args.warmup):
+        solve()
+    torch.cuda.synchronize()
+
+    kid = LB.KERNEL_ID[args.kernel]
+    LB.check(L.sph_profile_reset())
+    LB.check(L.sph_profile_enable(kid, 1))
+    clocks = ClockSampler(local)
+    if world > 1:
+        torch.distributed.barrier()
+    clocks.start()
+    torch.cuda.synchronize()
+    n0 = L.sph_launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = L.sph_launch_count() - n0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    kms, kn = C.c_double(), C.c_int64()
+    LB.check(L.sph_profile_read(kid, C.byref(kms), C.byref(kn)))
+    LB.check(L.sph_profile_enable(kid, 0))
+    rec = tape.recomputed_steps()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+
+    ps = N * args.nsteps * args.steps * world
+    value = ps / (ms / 1000.0)
+    esz = 4 if args.dtype == "f32" else 8
+    hbm, peak_kind = peaks()
+    per_launch_ms = kms.value / max(kn.value, 1)
+    algo_bytes = ALGO_WORDS[args.kernel] * esz * N
+    achieved = algo_bytes / (per_launch_ms / 1000.0) / 1e9
+    roof = {"kernel": args.kernel, "bound": "hbm", "achieved": achieved, "peak": hbm,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": args.traffic_bytes if args.traffic_bytes else None,
+            "algorithmic_bytes_per_launch": algo_bytes, "ms_per_launch": per_launch_ms,
+            "launches": kn.value}
+
+    # per-kernel breakdown of one more solve (untimed)
+    kernels = {}
+    if args.breakdown and rank == 0:
+        for k in LB.KERNELS:
+            L.sph_profile_enable(LB.KERNEL_ID[k], 1)
+        L.sph_profile_reset()
+        solve()
+        torch.cuda.synchronize()
+        for k in LB.KERNELS:
+            a, b = C.c_double(), C.c_int64()
+            L.sph_profile_read(LB.KERNEL_ID[k], C.byref(a), C.byref(b))
+            if b.value:
+                kernels[k] = {"ms": round(a.value, 3), "launches": b.value}
+            L.sph_profile_enable(LB.KERNEL_ID[k], 0)
+
+    # e2e: the reference-facing calls with host buffers
+    e2e = None
+    if args.e2e_steps > 0:
+        Xh = np.ascontiguousarray(X0.T, dtype=p.np)
+        Vh = np.ascontiguousarray(V0.T, dtype=p.np)
+        thh = np.asfortranarray(theta.astype(p.np))
+        outX = np.empty_like(Xh)
+        outV = np.empty_like(Vh)
+        gX = np.empty_like(Xh)
+        gV = np.empty_like(Vh)
+        gth = np.empty((p.ngx, p.ngy), p.np)
+
+        def solve_host():
+            h = C.c_void_p()
+            LB.check(L.sph_state_create(C.byref(pc), N, Xh.ctypes.data_as(C.c_void_p),
+                                        Vh.ctypes.data_as(C.c_void_p), p.code, 0.2, 4, 64,
+                                        C.byref(h)))
+            LB.check(L.sph_field_upload(th.h, thh.ctypes.data_as(C.c_void_p)))
+            tape.reset()
+            LB.check(L.sph_simulate(h, th.h, C.byref(pc), args.nsteps, tape.h, C.byref(flags)))
+            LB.check(L.sph_state_get(h, outX.ctypes.data_as(C.c_void_p),
+                                     outV.ctypes.data_as(C.c_void_p)))
+            right = outX[:, 0] > p.Lx / 2
+            sV = np.where(right[:, None], p.m * outV, 0).astype(p.np)
+            LB.check(L.sph_backward(ws.h, tape.h, th.h, C.byref(pc), None,
+                                    sV.ctypes.data_as(C.c_void_p), None, 0.2, 4, 64,
+                                    C.byref(flags)))
+            LB.check(L.sph_workspace_get(ws.h, gX.ctypes.data_as(C.c_void_p),
+                                         gV.ctypes.data_as(C.c_void_p),
+                                         gth.ctypes.data_as(C.c_void_p)))
+            LB.check(L.sph_state_destroy(h))
+
+        solve_host()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            solve_host()
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / args.e2e_steps
+        h2d = Xh.nbytes + Vh.nbytes + thh.nbytes + Vh.nbytes
+        d2h = outX.nbytes + outV.nbytes + gX.nbytes + gV.nbytes + gth.nbytes
+        e2e = {"value": N * args.nsteps * world / te, "unit": "particle-steps/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "ms_per_step": 1000 * te, "steps": args.e2e_steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and args.cpu_seconds > 0:
+        cpu = cpu_sample(p_d, X0, V0, theta, args.dtype, budget_s=args.cpu_seconds)
+        cpu.pop("seconds", None)
+
+    if rank == 0:
+        line = {"metric": "fwd+adjoint particle-steps/s", "value": value,
+                "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+                "data": "synthetic", "config": cfg, "roofline": roof, "cpu_baseline": cpu,
+                "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "recomputed_forward_steps_per_solve": rec,
+                "objective_J": J.value, "kernels_one_solve": kernels}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--side", type=int, default=1024, help="lattice side (particles = side^2)")
+    ap.add_argument("--nsteps", type=int, default=1000)
+    ap.add_argument("--snapshots", type=int, default=32)
+    ap.add_argument("--ntheta", type=int, default=256)
+    ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
+    ap.add_argument("--kernel", default="pass1", choices=sorted(ALGO_WORDS))
+    ap.add_argument("--traffic-bytes", type=float, default=0.0,
+                    help="ncu dram bytes per launch of --kernel, reported as roofline.traffic")
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=8.0)
+    ap.add_argument("--breakdown", type=int, default=1)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

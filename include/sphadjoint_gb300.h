@@ -143,6 +143,25 @@ SPH_API int32_t sph_backward(sph_workspace ws, sph_tape tp, sph_field theta,
 /* Array(ws.gX), Array(ws.gV), Array(ws.gtheta); any may be NULL */
 SPH_API int32_t sph_workspace_get(sph_workspace ws, void *gX, void *gV, void *gtheta);
 
+/* copyto!(dst, src) for whole States of the same configuration: positions,
+   velocities, permutation and neighbour structure (device to device) */
+SPH_API int32_t sph_state_assign(sph_state dst, sph_state src);
+
+/* On-device objectives (the reference evaluates them on the host after
+   Array(st.X)): J of the state's current (X, V), with the terminal seeds
+   dJ/dX_T, dJ/dV_T left in the workspace for sph_backward_seeded.
+   SPH_OBJ_TARGET is target_objective(X, xc, yc, sigma) (src/driver.jl:219-234),
+   args = {xc, yc, sigma}; SPH_OBJ_KE_RIGHT is the kinetic energy of the
+   particles with x > Lx/2 (args unused). J is summed in double in a fixed
+   order (deterministic). p may be NULL (the state's parameters). */
+enum { SPH_OBJ_KE_RIGHT = 0, SPH_OBJ_TARGET = 1 };
+SPH_API int32_t sph_objective(sph_workspace ws, sph_state st, int32_t kind, const double *args,
+                              const sph_params *p, double *J);
+/* backward! with the seeds of the last sph_objective on this workspace */
+SPH_API int32_t sph_backward_seeded(sph_workspace ws, sph_tape tp, sph_field theta,
+                                    const sph_params *p, sph_state scratch, double skin,
+                                    int32_t interval, int32_t maxnb, uint32_t *flags);
+
 /* ---- instrumentation ---- */
 /* kernels launched by this library since load */
 SPH_API int64_t sph_launch_count(void);

@@ -85,6 +85,9 @@ _SIGS = {
     "sph_workspace_destroy": (_I32, [_P]),
     "sph_backward": (_I32, [_P, _P, _P, _SP, _P, _P, _P, C.c_double, _I32, _I32, _U32P]),
     "sph_workspace_get": (_I32, [_P, _P, _P, _P]),
+    "sph_state_assign": (_I32, [_P, _P]),
+    "sph_objective": (_I32, [_P, _P, _I32, _DP, _SP, _DP]),
+    "sph_backward_seeded": (_I32, [_P, _P, _P, _SP, _P, C.c_double, _I32, _I32, _U32P]),
     "sph_launch_count": (_I64, []),
     "sph_profile_enable": (_I32, [_I32, _I32]),
     "sph_profile_read": (_I32, [_I32, _DP, _I64P]),

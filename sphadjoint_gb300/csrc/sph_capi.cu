@@ -430,6 +430,45 @@ SPH_API int32_t sph_backward(sph_workspace ws, sph_tape tp, sph_field theta, con
     });
 }
 
+SPH_API int32_t sph_state_assign(sph_state dst, sph_state src)
+{
+    return guarded([&] {
+        need(dst, "dst");
+        need(src, "src");
+        ST(dst)->assign(ST(src));
+    });
+}
+
+SPH_API int32_t sph_objective(sph_workspace ws, sph_state st, int32_t kind, const double *args,
+                              const sph_params *p, double *J)
+{
+    return guarded([&] {
+        need(ws, "workspace");
+        need(st, "state");
+        Params q;
+        if (p) q = to_params(p);
+        const double j = WS(ws)->objective(ST(st), kind, args, p ? &q : nullptr);
+        if (J) *J = j;
+    });
+}
+
+SPH_API int32_t sph_backward_seeded(sph_workspace ws, sph_tape tp, sph_field theta,
+                                    const sph_params *p, sph_state scratch, double skin,
+                                    int32_t interval, int32_t maxnb, uint32_t *flags)
+{
+    return guarded([&] {
+        need(ws, "workspace");
+        need(tp, "tape");
+        need(theta, "theta");
+        const Params q = to_params(p);
+        NLOpts o{skin, interval, maxnb};
+        if (o.interval < 1 || o.maxnb < 1) throw Error(ERR_ARG, "interval and maxnb must be positive");
+        uint32_t f = 0;
+        WS(ws)->backward_seeded(TP(tp), FD(theta), &q, scratch ? ST(scratch) : nullptr, o, &f);
+        if (flags) *flags = f;
+    });
+}
+
 SPH_API int32_t sph_workspace_get(sph_workspace ws, void *gX, void *gV, void *gtheta)
 {
     return guarded([&] { need(ws, "workspace"); WS(ws)->get(gX, gV, gtheta); });

@@ -536,6 +536,22 @@ template <typename T> class Sys final : public StateI {
         age = s.age;
         cellsOnlyLatest = false;
     }
+    void assign(StateI *src) override
+    {
+        auto *o = dynamic_cast<Sys<T> *>(src);
+        if (!o) throw Error(ERR_DTYPE, "source state has a different precision");
+        if (!same_config(*o)) throw Error(ERR_ARG, "source state has another configuration");
+        if (o == this) return;
+        pos[cur].copy_from(o->pos[o->cur]); vel[cur].copy_from(o->vel[o->cur]);
+        xref.copy_from(o->xref); perm.copy_from(o->perm); invperm.copy_from(o->invperm);
+        nbcount.copy_from(o->nbcount); cellStart.copy_from(o->cellStart);
+        center.copy_from(o->center); masks.copy_from(o->masks); flags.copy_from(o->flags);
+        rho.copy_from(o->rho); prho.copy_from(o->prho);
+        age = o->age;
+        prm = o->prm;
+        cellsOnlyLatest = false;
+    }
+
     bool same_config(const Sys &o) const
     {
         return N_ == o.N_ && nx == o.nx && ny == o.ny && opts.maxnb == o.opts.maxnb &&
@@ -569,6 +585,64 @@ template <typename T> void Sys<T>::neighbors(int32_t *indices, int32_t *nbc)
     if (indices) SPH_CK(cudaMemcpyAsync(indices, out.p, out.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
     if (nbc) SPH_CK(cudaMemcpyAsync(nbc, cnt.p, cnt.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
     SPH_CK(cudaStreamSynchronize(rt_stream()));
+}
+
+// ---------------------------------------------------------------------------
+// On-device objectives: J (deterministic block-ordered reduction in double)
+// and the terminal seeds dJ/dX_T, dJ/dV_T in particle-id order.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_objective(int64_t N, int kind, const int32_t *__restrict__ perm,
+                            const T2<T> *__restrict__ pos, const T2<T> *__restrict__ vel, T m,
+                            T Lx, T a0, T a1, T a2, T2<T> *__restrict__ seedX,
+                            T2<T> *__restrict__ seedV, double *__restrict__ partial)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double j = 0.0;
+    if (t < N) {
+        const int32_t id = perm[t];
+        const T2<T> x = pos[t], v = vel[t];
+        if (kind == OBJ_KE_RIGHT) {
+            const bool right = x.x > Lx / (T)2;
+            const T ke = (T)0.5 * m * (v.x * v.x + v.y * v.y);
+            j = right ? (double)ke : 0.0;
+            seedX[id] = mk2<T>((T)0, (T)0);
+            seedV[id] = right ? mk2<T>(m * v.x, m * v.y) : mk2<T>((T)0, (T)0);
+        } else {
+            // target_objective: e = exp(-|x - c|^2 / (2 sigma^2)), J -= e,
+            // seed = e * d / sigma^2
+            const T s2 = a2 * a2;
+            const T dx = x.x - a0, dy = x.y - a1;
+            const T e = exp(-(dx * dx + dy * dy) / ((T)2 * s2));
+            j = -(double)e;
+            seedX[id] = mk2<T>(e * dx / s2, e * dy / s2);
+            seedV[id] = mk2<T>((T)0, (T)0);
+        }
+    }
+    __shared__ double sm[kBlock];
+    sm[threadIdx.x] = j;
+    __syncthreads();
+    for (int o = kBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
+}
+
+// single block: fixed-order sum of the block partials
+static __global__ void k_sum_partials(int64_t nb, const double *__restrict__ partial,
+                                      double *__restrict__ out)
+{
+    __shared__ double sm[kBlock];
+    double a = 0.0;
+    for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) a += partial[i];
+    sm[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = kBlock / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) sm[threadIdx.x] += sm[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -692,8 +766,11 @@ template <typename T> class Work final : public WorkI {
     DevBuf<double> gtheta;
     DevBuf<T> gthetaT;
     DevBuf<T2<T>> outX, outV; // results in particle-id order
+    DevBuf<T2<T>> devSeedX, devSeedV; // seeds written by objective()
+    DevBuf<double> partial;
     std::unique_ptr<Sys<T>> own;
     bool haveResult = false;
+    bool haveDevSeeds = false;
 
     Work(int64_t N, const Params &p) : N_(N), ngx(p.ngx), ngy(p.ngy)
     {
@@ -742,7 +819,51 @@ template <typename T> class Work final : public WorkI {
     }
 
     void backward(TapeI *tape, FieldI *theta, const Params *p, const void *seedX,
-                  const void *seedV, StateI *scratch, NLOpts opts, uint32_t *flagsOut) override;
+                  const void *seedV, StateI *scratch, NLOpts opts, uint32_t *flags) override
+    {
+        run_backward(tape, theta, p, seedX, seedV, false, scratch, opts, flags);
+    }
+    void backward_seeded(TapeI *tape, FieldI *theta, const Params *p, StateI *scratch,
+                         NLOpts opts, uint32_t *flags) override
+    {
+        if (!haveDevSeeds) throw Error(ERR_STATE, "no objective has written seeds to this workspace");
+        run_backward(tape, theta, p, nullptr, nullptr, true, scratch, opts, flags);
+    }
+    void run_backward(TapeI *tape, FieldI *theta, const Params *p, const void *seedX,
+                      const void *seedV, bool devSeeds, StateI *scratch, NLOpts opts,
+                      uint32_t *flags);
+
+    double objective(StateI *sti, int kind, const double *args, const Params *pp) override
+    {
+        auto *st = dynamic_cast<Sys<T> *>(sti);
+        if (!st) throw Error(ERR_DTYPE, "state has a different precision than the workspace");
+        if (st->N_ != N_) throw Error(ERR_ARG, "state and workspace particle counts differ");
+        if (kind != OBJ_KE_RIGHT && kind != OBJ_TARGET) throw Error(ERR_ARG, "unknown objective");
+        if (kind == OBJ_TARGET && !args) throw Error(ERR_ARG, "target objective needs (xc, yc, sigma)");
+        const Params &q = pp ? *pp : st->prm;
+        const size_t n1 = (size_t)std::max<int64_t>(N_, 1);
+        if (!devSeedX.p) {
+            devSeedX.alloc(n1);
+            devSeedV.alloc(n1);
+            partial.alloc((size_t)grid_for(std::max<int64_t>(N_, 1)) + 1);
+        }
+        double J = 0.0;
+        if (N_) {
+            const T a0 = args ? (T)args[0] : (T)0, a1 = args ? (T)args[1] : (T)0,
+                    a2 = args ? (T)args[2] : (T)1;
+            SPH_LAUNCH(K_MISC, k_objective<T>, N_, N_, kind, st->perm.p, st->pos[st->cur].p,
+                       st->vel[st->cur].p, (T)q.m, (T)q.Lx, a0, a1, a2, devSeedX.p, devSeedV.p,
+                       partial.p);
+            const int64_t nb = grid_for(N_);
+            rt_before_launch(K_MISC);
+            k_sum_partials<<<1, kBlock, 0, rt_stream()>>>(nb, partial.p, partial.p + nb);
+            rt_after_launch(K_MISC);
+            SPH_CK(cudaMemcpyAsync(&J, partial.p + nb, sizeof(double), cudaMemcpyDeviceToHost, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
+        haveDevSeeds = true;
+        return J;
+    }
 
     void get(void *gXo, void *gVo, void *gth) override
     {
@@ -760,8 +881,9 @@ template <typename T> class Work final : public WorkI {
 };
 
 template <typename T>
-void Work<T>::backward(TapeI *tape, FieldI *theta, const Params *pp, const void *seedX,
-                       const void *seedV, StateI *scratch, NLOpts opts, uint32_t *flagsOut)
+void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const void *seedX,
+                           const void *seedV, bool devSeeds, StateI *scratch, NLOpts opts,
+                           uint32_t *flagsOut)
 {
     auto *tp = dynamic_cast<Tape<T> *>(tape);
     if (!tp) throw Error(ERR_DTYPE, "tape has a different precision than the workspace");
@@ -794,7 +916,10 @@ void Work<T>::backward(TapeI *tape, FieldI *theta, const Params *pp, const void 
 
     // seeds: copyto!(gX, seedX), copyto!(gV, seedV), id order -> S's cell order
     gcur = 0;
-    if (N_) {
+    if (N_ && devSeeds) {
+        SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, S->perm.p, devSeedX.p, gX[0].p);
+        SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, S->perm.p, devSeedV.p, gV[0].p);
+    } else if (N_) {
         if (seedX) {
             SPH_CK(cudaMemcpyAsync(stage2.p, seedX, stage2.bytes(), cudaMemcpyHostToDevice, rt_stream()));
             SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, S->perm.p, stage2.p, gX[0].p);

@@ -112,6 +112,12 @@ class StateI {
     virtual uint32_t take_flags() = 0;
     virtual void grid(int32_t *nx, int32_t *ny, double *cs, int64_t *age) const = 0;
     virtual void sync() = 0;
+    virtual void assign(StateI *src) = 0;
+};
+
+enum ObjectiveKind : int32_t {
+    OBJ_KE_RIGHT = 0, // J = sum 1/2 m |v|^2 over x > Lx/2
+    OBJ_TARGET = 1,   // target_objective(X, xc, yc, sigma) (src/driver.jl:219-234)
 };
 
 class WorkI {
@@ -123,6 +129,11 @@ class WorkI {
                           const void *seedV, StateI *scratch, NLOpts opts,
                           uint32_t *flags) = 0;
     virtual void get(void *gX, void *gV, void *gtheta) = 0;
+    // J of the state's current positions/velocities; the terminal seeds stay
+    // on the device for backward_seeded
+    virtual double objective(StateI *st, int kind, const double *args, const Params *p) = 0;
+    virtual void backward_seeded(TapeI *tape, FieldI *theta, const Params *p, StateI *scratch,
+                                 NLOpts opts, uint32_t *flags) = 0;
 };
 
 #define SPH_DECLARE_FACTORIES(SFX)                                                           \
