@@ -33,6 +33,8 @@ struct KTimer {
 KTimer g_timer[K_COUNT];
 } // namespace
 
+void set_last_error(const std::string &msg) { g_err = msg; }
+
 void cuda_check(cudaError_t e, const char *what)
 {
     if (e != cudaSuccess) {

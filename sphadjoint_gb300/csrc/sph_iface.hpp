@@ -44,6 +44,7 @@ enum Status : int32_t {
 };
 
 void cuda_check(cudaError_t e, const char *what);
+void set_last_error(const std::string &msg);
 #define SPH_CK(call) ::sphgb::cuda_check((call), #call)
 
 // ---- runtime ---------------------------------------------------------------

@@ -1,0 +1,70 @@
+"""CPU checks of the C ABI library: it loads without a GPU, exports every
+symbol the header declares, rejects bad arguments before touching the
+device, and its binomial checkpoint schedule is optimal (brute-force DP)."""
+import ctypes as C
+import functools
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "sphadjoint_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import sphadjoint_gb300 as S
+
+    return S.load()
+
+
+def declared_symbols():
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"SPH_API\s+[\w\s\*]+?\b(sph_\w+)\s*\(", txt)))
+
+
+def test_header_symbols_exported(lib):
+    names = declared_symbols()
+    assert len(names) > 30
+    raw = C.CDLL(lib._name)
+    for n in names:
+        assert hasattr(raw, n), n
+
+
+def test_bad_arguments_rejected_without_gpu(lib):
+    from sphadjoint_gb300 import _lib as LB
+
+    h = C.c_void_p()
+    p = LB.sph_params()
+    assert lib.sph_state_create(None, 4, None, None, 0, 0.2, 4, 64, C.byref(h)) == 1
+    assert b"params" in lib.sph_last_error()
+    assert lib.sph_state_create(C.byref(p), 4, None, None, 7, 0.2, 4, 64, C.byref(h)) == 4
+    assert lib.sph_tape_create_checkpointed(4, 10, 0, 0, C.byref(h)) == 1
+    assert lib.sph_simulate(None, None, None, 1, None, None) == 1
+    assert lib.sph_version() >= 100
+
+
+@functools.lru_cache(maxsize=None)
+def dp_cost(l, c):
+    """Brute force: forward steps to reverse l steps with c slots, the state at
+    the start held in one of them (recursive split, every m tried)."""
+    if l <= 1:
+        return 0
+    if c <= 1:
+        return l * (l - 1) // 2
+    return min(m + dp_cost(l - m, c - 1) + dp_cost(m, c) for m in range(1, l))
+
+
+@pytest.mark.parametrize("c", [1, 2, 3, 4, 6])
+def test_checkpoint_schedule_is_optimal(lib, c):
+    for l in range(1, 61):
+        assert lib.sph_plan_cost(l, c) == dp_cost(l, c), (l, c)
+        if l > 1 and c > 1:
+            m = lib.sph_plan_split(l, c)
+            assert m + dp_cost(l - m, c - 1) + dp_cost(m, c) == dp_cost(l, c)
+
+
+def test_checkpoint_cost_of_the_benchmark_horizon(lib):
+    # 1000 steps, 32 snapshots: repetition number 3, 3*1000 - C(35, 2) = 2405
+    assert lib.sph_plan_cost(1000, 32) == 2405
