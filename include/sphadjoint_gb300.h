@@ -162,6 +162,27 @@ SPH_API int32_t sph_backward_seeded(sph_workspace ws, sph_tape tp, sph_field the
                                     const sph_params *p, sph_state scratch, double skin,
                                     int32_t interval, int32_t maxnb, uint32_t *flags);
 
+/* ---- cell list without allocation ----
+   No counterpart in the reference. build!(cl, X, p, backend)
+   (src/neighbors.jl:97-114) for callers that cannot let a library allocate
+   device memory (their arrays come from their own pool or budgeted
+   allocator). X_dev: N positions, interleaved T on the device; outputs are
+   caller-owned device arrays: counts[nx*ny], starts[nx*ny] (0-based),
+   order[N] (1-based ids, ascending within each cell), exactly as sph_build_cells
+   + sph_get_celllist give them. cs is CellList.cs, nx/ny its grid. Work
+   arrays live in a fixed device array (about 16 MiB per GPU, held until
+   exit), so N <= SPH_NOALLOC_MAX_PARTICLES and nx*ny <= SPH_NOALLOC_MAX_CELLS;
+   larger sizes return SPH_ERR_ARG. Calls no cudaMalloc/cudaFree. Enqueued on
+   `stream` (a cudaStream_t, NULL = legacy default) and not synchronised.
+   All calls share the work array: calls that overlap on the GPU race, so
+   serialise them. The first call on each device resolves the array's address
+   (cudaGetSymbolAddress): make it before any stream capture. */
+#define SPH_NOALLOC_MAX_PARTICLES (1 << 20)
+#define SPH_NOALLOC_MAX_CELLS (1 << 20)
+SPH_API int32_t sph_build_cells_noalloc(const void *X_dev, int64_t N, int32_t dtype, double cs,
+                                        int32_t nx, int32_t ny, int32_t *counts_dev,
+                                        int32_t *starts_dev, int32_t *order_dev, void *stream);
+
 /* ---- instrumentation ---- */
 /* kernels launched by this library since load */
 SPH_API int64_t sph_launch_count(void);

@@ -25,6 +25,7 @@ SOURCES = {
     "sph_f64.cu": ["--fmad=false"],
     "sph_f32.cu": ["--fmad=true"],
     "sph_capi.cu": [],
+    "sph_noalloc.cu": ["--fmad=false"],
 }
 DEPS = ["sph_common.cuh", "sph_kernels.cuh", "sph_engine.cuh", "sph_iface.hpp"]
 
