@@ -241,7 +241,7 @@ def run_ours(args):
 
     kid = LB.KERNEL_ID[args.kernel]
     LB.check(L.sph_profile_reset())
-    LB.check(L.sph_profile_enable(kid, 1))
+    LB.check(L.sph_profile_enable(kid, int(args.kernel_events)))
     clocks = ClockSampler(local)
     if world > 1:
         torch.distributed.barrier()
@@ -271,12 +271,22 @@ def run_ours(args):
     value = ps / (ms / 1000.0)
     esz = 4 if args.dtype == "f32" else 8
     hbm, peak_kind = peaks()
+    if not args.kernel_events:
+        # the timed region ran without per-launch events; time the kernel on
+        # one more solve instead
+        LB.check(L.sph_profile_reset())
+        LB.check(L.sph_profile_enable(kid, 1))
+        solve()
+        torch.cuda.synchronize()
+        LB.check(L.sph_profile_read(kid, C.byref(kms), C.byref(kn)))
+        LB.check(L.sph_profile_enable(kid, 0))
     per_launch_ms = kms.value / max(kn.value, 1)
     algo_bytes = ALGO_WORDS[args.kernel] * esz * N
     achieved = algo_bytes / (per_launch_ms / 1000.0) / 1e9
     roof = {"kernel": args.kernel, "bound": "hbm", "achieved": achieved, "peak": hbm,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": args.traffic_bytes if args.traffic_bytes else None,
+            "traffic": (args.traffic_bytes if args.traffic_bytes and args.kernel == "pass1"
+                        and N == 1 << 20 else None),
             "algorithmic_bytes_per_launch": algo_bytes, "ms_per_launch": per_launch_ms,
             "launches": kn.value}
 
@@ -371,8 +381,13 @@ def main():
     ap.add_argument("--ntheta", type=int, default=256)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--kernel", default="pass1", choices=sorted(ALGO_WORDS))
-    ap.add_argument("--traffic-bytes", type=float, default=0.0,
-                    help="ncu dram bytes per launch of --kernel, reported as roofline.traffic")
+    ap.add_argument("--kernel-events", type=int, default=1,
+                    help="time --kernel with CUDA events inside the timed region (1) or on "
+                         "one extra solve after it (0)")
+    ap.add_argument("--traffic-bytes", type=float, default=80.70e6,
+                    help="ncu dram read+write bytes of one launch of --kernel at the default "
+                         "size (k_pass1_design, 1,048,576 particles: 76.11 MB + 4.59 MB), "
+                         "reported as roofline.traffic; 0 = unknown")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)

@@ -84,18 +84,34 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, int64_t i,
     const int cy = (int)((cc >> 16) & 0x7fffu);
     const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
     if (!(cc >> 31)) {
-#pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            uint64_t m = v.masks[(int64_t)r * v.N + i];
-            if (m) {
-                const int jy = cy + r - 1;
-                const int64_t b = v.cellStart[(int64_t)(jx0 - 1) + (int64_t)(jy - 1) * v.nx];
-                do {
-                    const int k = __ffsll((long long)m) - 1;
-                    m &= m - 1;
-                    f(b + k);
-                } while (m);
+        // Slot indices fit in 32 bits (N < 2^31). The three row masks are
+        // walked as one sequence of six 32-bit words (row 0 low, row 0 high,
+        // row 1 low, ...), bit order = slot order, in a single loop: a lane
+        // that runs out of bits in one word moves to its next word while the
+        // others keep visiting neighbours, so a warp pays for its largest
+        // total neighbour count rather than the sum of its per-row maxima.
+        const int row0 = (jx0 - 1) + (cy - 2) * v.nx; // cell (jx0, cy - 1), 0-based
+        const uint64_t m0 = v.masks[i];
+        const uint64_t m1 = v.masks[v.N + i];
+        const uint64_t m2 = v.masks[2 * v.N + i];
+        const int b0 = m0 ? v.cellStart[row0] : 0;
+        const int b1 = m1 ? v.cellStart[row0 + v.nx] : 0;
+        const int b2 = m2 ? v.cellStart[row0 + 2 * v.nx] : 0;
+        uint32_t m = (uint32_t)m0;
+        int base = b0;
+        int w = 0;
+        for (;;) {
+            if (m == 0u) {
+                if (++w == 6) break;
+                const uint64_t mr = w < 2 ? m0 : (w < 4 ? m1 : m2);
+                const int br = w < 2 ? b0 : (w < 4 ? b1 : b2);
+                m = (w & 1) ? (uint32_t)(mr >> 32) : (uint32_t)mr;
+                base = br + ((w & 1) << 5);
+                continue;
             }
+            const int k = __ffs((int)m) - 1;
+            m &= m - 1u;
+            f(base + k);
         }
     } else {
         const int jx1 = cx + 1 < v.nx ? cx + 1 : v.nx;
@@ -120,6 +136,12 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, int64_t i,
         }
     }
 }
+
+// Per-pair square root and reciprocal. FP64 keeps IEEE sqrt and division
+// (reference-exact); FP32 uses the hardware reciprocal square root, which is
+// within a few ulp (the FP32 path is checked against FP64 by tolerance).
+__device__ __forceinline__ double pair_sqrt(double r2) { return sqrt(r2); }
+__device__ __forceinline__ float pair_sqrt(float r2) { return r2 > 0.f ? r2 * rsqrtf(r2) : 0.f; }
 
 // clamp(unsafe_trunc(Int, floor(v)) + 2, 1, n) (src/neighbors.jl:38-42,217-218).
 // The float clamp keeps the conversion defined; no finite result changes.

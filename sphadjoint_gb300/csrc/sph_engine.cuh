@@ -569,7 +569,7 @@ __global__ void k_list_neighbors(NLView<T> v, const int32_t *__restrict__ perm,
     if (i >= v.N) return;
     const int32_t id = perm[i];
     int m = 0;
-    for_each_neighbor<T>(v, i, [&](int64_t j) {
+    for_each_neighbor<T>(v, i, [&](int j) {
         out[(int64_t)id * v.maxnb + m] = perm[j] + 1;
         ++m;
     });

@@ -230,19 +230,21 @@ __global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2,
     bool over = false;
 #pragma unroll
     for (int r = 0; r < 3; ++r) {
-        uint64_t mk = 0;
+        uint32_t lo = 0, hi = 0;
         const int jy = cy + r - 1;
         if (jy >= 1 && jy <= ny) {
-            const int64_t row = (int64_t)(jy - 1) * nx;
-            const int64_t b = cellStart[row + jx0 - 1];
-            const int64_t e = cellStart[row + jx1];
+            const int row = (jy - 1) * nx;
+            const int b = cellStart[row + jx0 - 1];
+            const int e = cellStart[row + jx1];
             if (e - b > 64) spill = 1;
-            for (int64_t j = b; j < e; ++j) {
+            for (int j = b; j < e; ++j) {
                 const T2<T> xj = pos[j];
                 const T r2 = r2_exact<T>(sub_rn(xi.x, xj.x), sub_rn(xi.y, xj.y));
                 if (r2min < r2 && r2 < rc2) {
                     if (m < maxnb) {
-                        if (j - b < 64) mk |= 1ull << (j - b);
+                        const int k = j - b;
+                        if (k < 32) lo |= 1u << k;
+                        else if (k < 64) hi |= 1u << (k - 32);
                         ++m;
                     } else {
                         over = true;
@@ -250,7 +252,7 @@ __global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2,
                 }
             }
         }
-        masks[(int64_t)r * N + i] = mk;
+        masks[(int64_t)r * N + i] = ((uint64_t)hi << 32) | lo;
     }
     center[i] = (uint32_t)cx | ((uint32_t)cy << 16) | (spill << 31);
     nbcount[i] = m;
@@ -271,13 +273,13 @@ __global__ void __launch_bounds__(kBlock) k_density_eos(NLView<T> v, Phys<T> p,
     if (i >= v.N) return;
     const T2<T> xi = v.pos[i];
     T acc = (T)0;
-    for_each_neighbor<T>(v, i, [&](int64_t j) {
+    for_each_neighbor<T>(v, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < p.r2max) {
-            const T q = sqrt(r2) * p.invh;
+            const T q = pair_sqrt(r2) * p.invh;
             const T u = (T)1 - (T)0.5 * q;
             const T u2 = u * u;
             acc += p.m * (p.A * u2 * u2 * ((T)2 * q + (T)1));
@@ -301,13 +303,13 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Phys<T> &p,
     const T pti = pi.x, iri = pi.y;
     ax = (T)0;
     ay = (T)0;
-    for_each_neighbor<T>(v, i, [&](int64_t j) {
+    for_each_neighbor<T>(v, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < p.r2max) {
-            const T q = sqrt(r2) * p.invh;
+            const T q = pair_sqrt(r2) * p.invh;
             const T u = (T)1 - (T)0.5 * q;
             const T F = p.Fc * u * u * u;
             const T2<T> pj = prho[j];
@@ -481,13 +483,19 @@ __global__ void __launch_bounds__(kBlock)
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
     T gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
-    for_each_neighbor<T>(v, i, [&](int64_t j) {
+    for_each_neighbor<T>(v, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < p.r2max) {
-            const T r = sqrt(r2);
+            T r, rinv;
+            if constexpr (sizeof(T) == 4) {
+                rinv = r2 > (T)0 ? rsqrtf(r2) : (T)0;
+                r = r2 * rinv;
+            } else {
+                r = sqrt(r2);
+            }
             const T q = r * p.invh;
             const T u = (T)1 - (T)0.5 * q;
             const T F = p.Fc * u * u * u;
@@ -507,7 +515,9 @@ __global__ void __launch_bounds__(kBlock)
             gx -= Pij * F * dax;
             gy -= Pij * F * day;
             const T Fbar = Pij * ad_d + Cbase * ad_v;
-            const T w = Fbar * G * p.invh / r;
+            T w;
+            if constexpr (sizeof(T) == 4) w = Fbar * G * p.invh * rinv;
+            else w = Fbar * G * p.invh / r;
             gx += w * dx;
             gy += w * dy;
             gvx += C * dax;
@@ -574,13 +584,13 @@ __global__ void __launch_bounds__(kBlock)
     const T2<T> xi = v.pos[i];
     const T gri = grho[i];
     T gx = 0, gy = 0;
-    for_each_neighbor<T>(v, i, [&](int64_t j) {
+    for_each_neighbor<T>(v, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < p.r2max) {
-            const T q = sqrt(r2) * p.invh;
+            const T q = pair_sqrt(r2) * p.invh;
             const T u = (T)1 - (T)0.5 * q;
             const T w = p.m * (p.Fc * u * u * u) * (gri + grho[j]);
             gx += w * dx;
