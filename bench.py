@@ -72,6 +72,121 @@ def workload(n_side=1024, nsteps=1000, snapshots=32, ntheta=256, dtype="f32"):
     return p, X0, V0, theta, cfg
 
 
+def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3):
+    """64 independent dam breaks: N log-uniform in [1k, 64k], aspect (height /
+    width of the water block) uniform in [0.3, 1.0], each with its own seeded,
+    box-smoothed 64 x 64 theta; dx = 1e-3, tank 2W x 1.25 max(W, H)."""
+    rng = np.random.default_rng(seed)
+    dx = 1e-3
+    inst = []
+    for b in range(B):
+        n = int(round(math.exp(rng.uniform(math.log(1000), math.log(64000)))))
+        aspect = rng.uniform(0.3, 1.0)
+        nx = max(2, int(round(math.sqrt(n / aspect))))
+        ny = max(2, int(round(n / nx)))
+        W, H = nx * dx, ny * dx
+        h = 1.3 * dx
+        c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+        p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0,
+                 Lx=2.0 * W, Ly=1.25 * max(W, H), kw=5e4, ngx=ntheta, ngy=ntheta)
+        xs = dx + dx * np.arange(nx)
+        ys = dx + dx * np.arange(ny)
+        X, Y = np.meshgrid(xs, ys)
+        X0 = np.vstack([X.ravel(), Y.ravel()]) + rng.uniform(-0.05 * dx, 0.05 * dx, (2, nx * ny))
+        t = rng.random((ntheta, ntheta))
+        pad = np.pad(t, 2, mode="edge")
+        theta = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
+        inst.append((p, X0, np.zeros_like(X0), theta))
+    cfg = {"workload": f"batched: {B} dam breaks, N log-uniform in [1k, 64k], aspect in [0.3, 1], "
+                       f"own {ntheta}x{ntheta} theta each, {nsteps} steps FP32, full tape",
+           "instances": B, "particles": int(sum(x[1].shape[1] for x in inst)),
+           "time_steps": nsteps, "theta": [ntheta, ntheta], "dx": dx,
+           "skin": 0.2, "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half"}
+    return inst, cfg
+
+
+def run_batched(args):
+    """Packed batch (one launch per kernel for all instances) vs the same
+    solves run one after another, one solve per launch sequence."""
+    import torch
+    import sphadjoint_gb300 as S
+    from sphadjoint_gb300 import _lib as LB
+
+    torch.cuda.set_device(0)
+    L = S.load()
+    stream = torch.cuda.Stream()
+    LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
+    inst, cfg = batched_workload(args.instances, args.nsteps)
+    ps = [S.SPHParams(**p, dtype=args.dtype) for p, _, _, _ in inst]
+    ntot = sum(x[1].shape[1] for x in inst)
+    flags = C.c_uint32()
+
+    bt0 = S.Batch([x[1] for x in inst], [x[2] for x in inst], ps)
+    bt = S.Batch([x[1] for x in inst], [x[2] for x in inst], ps)
+    th = S.BatchField([x[3] for x in inst], args.dtype)
+    tape = S.Tape(ntot, args.nsteps, ps[0], snapshots=args.snapshots)
+    ws = S.BatchWorkspace(bt)
+    Jb = (C.c_double * len(inst))()
+
+    def solve_batch():
+        LB.check(L.sph_state_assign(bt.h, bt0.h))
+        tape.reset()
+        LB.check(L.sph_simulate(bt.h, th.h, None, args.nsteps, tape.h, C.byref(flags)))
+        LB.check(L.sph_batch_objective(ws.h, bt.h, 0, None, Jb))
+        LB.check(L.sph_backward_seeded(ws.h, tape.h, th.h, None, None, 0.2, 4, 64, C.byref(flags)))
+
+    def timed(fn, reps):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n0 = L.sph_launch_count()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps, (L.sph_launch_count() - n0) / reps
+
+    ms_b, launches_b = timed(solve_batch, args.steps)
+    del tape
+
+    # the same instances, one solve at a time
+    solo = []
+    for p, X0, V0, theta in inst:
+        pp = S.SPHParams(**p, dtype=args.dtype)
+        n = X0.shape[1]
+        s0 = S.State(X0, V0, pp)
+        s1 = S.State(X0, V0, pp)
+        f = S.DesignField(theta, args.dtype)
+        tp = S.Tape(n, args.nsteps, pp, snapshots=args.snapshots)
+        w = S.AdjointWorkspace(n, pp)
+        solo.append((pp, s0, s1, f, tp, w))
+    Js = C.c_double()
+
+    def solve_plain():
+        for pp, s0, s1, f, tp, w in solo:
+            pc = pp.c_struct()
+            LB.check(L.sph_state_assign(s1.h, s0.h))
+            tp.reset()
+            LB.check(L.sph_simulate(s1.h, f.h, C.byref(pc), args.nsteps, tp.h, C.byref(flags)))
+            LB.check(L.sph_objective(w.h, s1.h, 0, None, C.byref(pc), C.byref(Js)))
+            LB.check(L.sph_backward_seeded(w.h, tp.h, f.h, C.byref(pc), None, 0.2, 4, 64,
+                                           C.byref(flags)))
+
+    ms_p, launches_p = timed(solve_plain, max(1, args.steps // 2))
+    ps_total = ntot * args.nsteps
+    line = {"metric": "fwd+adjoint particle-steps/s (batched vs one solve per launch)",
+            "value": ps_total / (ms_b / 1000.0), "unit": "particle-steps/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_b,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.dtype, "data": "synthetic", "config": cfg,
+            "plain": {"value": ps_total / (ms_p / 1000.0), "ms_per_step": ms_p,
+                      "gpu_launches_per_step": launches_p},
+            "speedup_vs_plain": ms_p / ms_b, "gpu_launches": launches_b}
+    print(json.dumps(line))
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -375,6 +490,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="single", choices=["single", "batched"])
+    ap.add_argument("--instances", type=int, default=64, help="batched: number of instances")
     ap.add_argument("--side", type=int, default=1024, help="lattice side (particles = side^2)")
     ap.add_argument("--nsteps", type=int, default=1000)
     ap.add_argument("--snapshots", type=int, default=32)
@@ -395,6 +512,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 

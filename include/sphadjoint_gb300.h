@@ -157,10 +157,38 @@ SPH_API int32_t sph_state_assign(sph_state dst, sph_state src);
 enum { SPH_OBJ_KE_RIGHT = 0, SPH_OBJ_TARGET = 1 };
 SPH_API int32_t sph_objective(sph_workspace ws, sph_state st, int32_t kind, const double *args,
                               const sph_params *p, double *J);
-/* backward! with the seeds of the last sph_objective on this workspace */
+/* backward! with the seeds of the last sph_objective on this workspace (p may be
+   NULL for a batch) */
 SPH_API int32_t sph_backward_seeded(sph_workspace ws, sph_tape tp, sph_field theta,
                                     const sph_params *p, sph_state scratch, double skin,
                                     int32_t interval, int32_t maxnb, uint32_t *flags);
+
+/* ---- batches ----
+   No counterpart in the reference (one State per call there). B independent
+   instances (their own SPHParams, particle counts, cell grids and design
+   fields; shared neighbour-list knobs) packed into one State, design field and
+   workspace, so every kernel of step!/simulate!/backward! runs once for all of
+   them. Host arrays are packed: instance b's particles occupy ids
+   [off_b, off_b + N[b]) with off_b = N[0] + ... + N[b-1]; its theta block
+   ((ngy_b, ngx_b) column-major) follows instance b-1's. Each instance's
+   results equal those of the same instance run alone (bit for bit in FP64).
+   Use the State/Tape/workspace calls above on the packed handles (p = NULL:
+   each instance keeps its own parameters; a tape is created for the total
+   particle count). */
+SPH_API int32_t sph_batch_create(int32_t B, const sph_params *params, const int64_t *N,
+                                 const void *X0, const void *V0, int32_t dtype, double skin,
+                                 int32_t interval, int32_t maxnb, sph_state *out);
+SPH_API int32_t sph_batch_field_create(int32_t B, const int32_t *ngx, const int32_t *ngy,
+                                       int32_t dtype, const void *theta, sph_field *out);
+SPH_API int32_t sph_batch_workspace_create(int32_t B, const sph_params *params, const int64_t *N,
+                                           int32_t dtype, sph_workspace *out);
+SPH_API int32_t sph_batch_size(sph_state st, int32_t *B);
+/* per-instance neighbour-list flags, flags[B] (read and cleared) */
+SPH_API int32_t sph_batch_take_flags(sph_state st, uint32_t *flags);
+/* per-instance objective J[B]; args: 3 values (xc, yc, sigma) per instance for
+   SPH_OBJ_TARGET, NULL for SPH_OBJ_KE_RIGHT. Seeds stay in the workspace. */
+SPH_API int32_t sph_batch_objective(sph_workspace ws, sph_state st, int32_t kind,
+                                    const double *args, double *J);
 
 /* ---- cell list without allocation ----
    No counterpart in the reference. build!(cl, X, p, backend)

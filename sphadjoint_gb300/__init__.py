@@ -4,7 +4,11 @@
 reference's Julia API over that ABI."""
 from .api import (  # noqa: F401
     AdjointWorkspace,
+    Batch,
+    BatchField,
+    BatchWorkspace,
     DesignField,
+    batch_backward,
     SPHParams,
     State,
     Tape,

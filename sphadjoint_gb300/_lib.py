@@ -88,6 +88,12 @@ _SIGS = {
     "sph_state_assign": (_I32, [_P, _P]),
     "sph_objective": (_I32, [_P, _P, _I32, _DP, _SP, _DP]),
     "sph_backward_seeded": (_I32, [_P, _P, _P, _SP, _P, C.c_double, _I32, _I32, _U32P]),
+    "sph_batch_create": (_I32, [_I32, _SP, _I64P, _P, _P, _I32, C.c_double, _I32, _I32, _PP]),
+    "sph_batch_field_create": (_I32, [_I32, _I32P, _I32P, _I32, _P, _PP]),
+    "sph_batch_workspace_create": (_I32, [_I32, _SP, _I64P, _I32, _PP]),
+    "sph_batch_size": (_I32, [_P, _I32P]),
+    "sph_batch_take_flags": (_I32, [_P, _U32P]),
+    "sph_batch_objective": (_I32, [_P, _P, _I32, _DP, _DP]),
     "sph_launch_count": (_I64, []),
     "sph_profile_enable": (_I32, [_I32, _I32]),
     "sph_profile_read": (_I32, [_I32, _DP, _I64P]),

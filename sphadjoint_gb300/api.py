@@ -291,6 +291,146 @@ class AdjointWorkspace:
         return self.get()[2]
 
 
+class Batch:
+    """B independent instances packed into one State (no counterpart in the
+    reference, which runs one State per call). Each instance keeps its own
+    SPHParams, particle count, cell grid and design field; step/simulate/
+    backward run every kernel once for all of them, and each instance's
+    results equal those of the same instance run alone.
+
+    ``X0s``/``V0s`` are lists of (2, N_b) arrays; ``params`` a list of
+    SPHParams (one dtype for all).
+    """
+
+    def __init__(self, X0s, V0s, params, skin=0.2, interval=4, maxnb=64):
+        self._L = L.load()
+        self.params = list(params)
+        p0 = self.params[0]
+        if any(p.dtype != p0.dtype for p in self.params):
+            raise ValueError("all instances of a batch share one dtype")
+        self.p = p0
+        self.B = len(self.params)
+        self.sizes = [int(np.asarray(x).size // 2) for x in X0s]
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
+        self.N = int(self.offsets[-1])
+        self.maxnb = int(maxnb)
+        X = np.concatenate([_xy(x, n, p0.np) for x, n in zip(X0s, self.sizes)]) if self.N else \
+            np.zeros((0, 2), p0.np)
+        V = np.concatenate([_xy(v, n, p0.np) for v, n in zip(V0s, self.sizes)]) if self.N else \
+            np.zeros((0, 2), p0.np)
+        cps = (L.sph_params * self.B)(*[q.c_struct() for q in self.params])
+        ns = (C.c_int64 * self.B)(*self.sizes)
+        h = C.c_void_p()
+        L.check(self._L.sph_batch_create(self.B, cps, ns, _ptr(np.ascontiguousarray(X)),
+                                         _ptr(np.ascontiguousarray(V)), p0.code, float(skin),
+                                         int(interval), int(maxnb), C.byref(h)))
+        self.h = h
+        self.last_flags = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_state_destroy(self.h)
+            self.h = None
+
+    def get(self):
+        """[(X_b, V_b)] with (2, N_b) arrays."""
+        X = np.empty((self.N, 2), self.p.np)
+        V = np.empty((self.N, 2), self.p.np)
+        L.check(self._L.sph_state_get(self.h, _ptr(X), _ptr(V)))
+        o = self.offsets
+        return [(X[o[b]:o[b + 1]].T, V[o[b]:o[b + 1]].T) for b in range(self.B)]
+
+    def take_flags(self):
+        f = (C.c_uint32 * self.B)()
+        L.check(self._L.sph_batch_take_flags(self.h, f))
+        return list(f)
+
+
+class BatchField(DesignField):
+    """The design fields of a batch, one (ngy_b, ngx_b) array per instance."""
+
+    def __init__(self, thetas, dtype: str = "f64"):
+        self._L = L.load()
+        code, npdt = _DT[dtype]
+        ths = [np.asarray(t, dtype=np.float64) for t in thetas]
+        self.dtype = dtype
+        self.shapes = [t.shape for t in ths]
+        self.shape = self.shapes[0]
+        B = len(ths)
+        gy = (C.c_int32 * B)(*[t.shape[0] for t in ths])
+        gx = (C.c_int32 * B)(*[t.shape[1] for t in ths])
+        packed = np.concatenate([np.asfortranarray(t.astype(npdt)).ravel(order="F") for t in ths])
+        h = C.c_void_p()
+        L.check(self._L.sph_batch_field_create(B, gx, gy, code, _ptr(packed), C.byref(h)))
+        self.h = h
+
+
+class BatchWorkspace:
+    """AdjointWorkspace for a Batch."""
+
+    def __init__(self, batch: Batch):
+        self._L = L.load()
+        self.B, self.N, self.p = batch.B, batch.N, batch.p
+        self.params, self.sizes, self.offsets = batch.params, batch.sizes, batch.offsets
+        cps = (L.sph_params * self.B)(*[q.c_struct() for q in self.params])
+        ns = (C.c_int64 * self.B)(*self.sizes)
+        h = C.c_void_p()
+        L.check(self._L.sph_batch_workspace_create(self.B, cps, ns, self.p.code, C.byref(h)))
+        self.h = h
+        self.last_flags = 0
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_workspace_destroy(self.h)
+            self.h = None
+
+    def get(self):
+        """[(gX_b, gV_b, gtheta_b)] per instance."""
+        gX = np.empty((self.N, 2), self.p.np)
+        gV = np.empty((self.N, 2), self.p.np)
+        nn = [q.ngx * q.ngy for q in self.params]
+        gt = np.empty(sum(nn), self.p.np)
+        L.check(self._L.sph_workspace_get(self.h, _ptr(gX), _ptr(gV), _ptr(gt)))
+        o = self.offsets
+        out, t0 = [], 0
+        for b, q in enumerate(self.params):
+            g = gt[t0:t0 + nn[b]].reshape(q.ngx, q.ngy).T
+            out.append((gX[o[b]:o[b + 1]].T, gV[o[b]:o[b + 1]].T, g))
+            t0 += nn[b]
+        return out
+
+    def objective(self, batch: Batch, kind="ke_right", args=None):
+        J = (C.c_double * self.B)()
+        k = {"ke_right": 0, "target": 1}[kind]
+        a = None
+        if args is not None:
+            arr = np.ascontiguousarray(np.asarray(args, np.float64).reshape(self.B, 3))
+            a = arr.ctypes.data_as(C.POINTER(C.c_double))
+        L.check(self._L.sph_batch_objective(self.h, batch.h, k, a, J))
+        return np.array(J[:])
+
+
+def batch_backward(ws: BatchWorkspace, tape: Tape, theta: BatchField, seedsX=None, seedsV=None,
+                   scratch=None, skin=0.2, interval=4, maxnb=64, seeded=False):
+    """backward! over a Batch: seeds are lists of (2, N_b) arrays (or, with
+    seeded=True, the seeds left by BatchWorkspace.objective)."""
+    f = C.c_uint32()
+    if seeded:
+        L.check(ws._L.sph_backward_seeded(ws.h, tape.h, theta.h, None,
+                                          scratch.h if scratch is not None else None, float(skin),
+                                          int(interval), int(maxnb), C.byref(f)))
+    else:
+        dt = ws.p.np
+        sx = np.concatenate([_xy(a, n, dt) for a, n in zip(seedsX, ws.sizes)]) if seedsX else None
+        sv = np.concatenate([_xy(a, n, dt) for a, n in zip(seedsV, ws.sizes)]) if seedsV else None
+        L.check(ws._L.sph_backward(ws.h, tape.h, theta.h, None, _ptr(sx), _ptr(sv),
+                                   scratch.h if scratch is not None else None, float(skin),
+                                   int(interval), int(maxnb), C.byref(f)))
+    ws.last_flags = f.value
+    _warn_flags(f.value, maxnb)
+    return ws
+
+
 def reset(tape: Tape) -> Tape:
     """reset!(tape) (src/driver.jl:71)."""
     return tape.reset()
@@ -316,8 +456,9 @@ def step(st: State, theta, p: SPHParams | None = None) -> State:
 
 
 def simulate(st: State, theta, p: SPHParams | None, nsteps: int, tape: Tape | None = None) -> State:
-    """simulate!(st, theta, p, backend, nsteps; tape) (src/driver.jl:92-115)."""
-    th = _field(theta, st.p)
+    """simulate!(st, theta, p, backend, nsteps; tape) (src/driver.jl:92-115).
+    Also runs a Batch (p = None, theta a BatchField)."""
+    th = theta if isinstance(theta, DesignField) else _field(theta, st.p)
     f = C.c_uint32()
     L.check(st._L.sph_simulate(st.h, th.h, C.byref(p.c_struct()) if p is not None else None,
                                int(nsteps), tape.h if tape is not None else None, C.byref(f)))

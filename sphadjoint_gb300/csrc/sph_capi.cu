@@ -220,8 +220,8 @@ SPH_API int32_t sph_field_create(int32_t ngx, int32_t ngy, int32_t dtype, const 
     return guarded([&] {
         need(out, "out");
         check_dtype(dtype);
-        FieldI *f = dtype == SPH_F64 ? make_field_f64(ngx, ngy, theta)
-                                     : make_field_f32(ngx, ngy, theta);
+        const std::vector<int> gx{ngx}, gy{ngy};
+        FieldI *f = dtype == SPH_F64 ? make_field_f64(gx, gy, theta) : make_field_f32(gx, gy, theta);
         *out = reinterpret_cast<sph_field>(f);
     });
 }
@@ -258,8 +258,10 @@ SPH_API int32_t sph_state_create(const sph_params *p, int64_t N, const void *X0,
         check_dtype(dtype);
         const Params q = to_params(p);
         NLOpts o{skin, interval, maxnb};
-        StateI *s = dtype == SPH_F64 ? make_state_f64(q, N, X0, V0, o)
-                                     : make_state_f32(q, N, X0, V0, o);
+        const std::vector<Params> ps{q};
+        const std::vector<int64_t> ns{N};
+        StateI *s = dtype == SPH_F64 ? make_state_f64(ps, ns, X0, V0, o)
+                                     : make_state_f32(ps, ns, X0, V0, o);
         *out = reinterpret_cast<sph_state>(s);
     });
 }
@@ -405,7 +407,9 @@ SPH_API int32_t sph_workspace_create(int64_t N, const sph_params *p, int32_t dty
         need(out, "out");
         check_dtype(dtype);
         const Params q = to_params(p);
-        WorkI *w = dtype == SPH_F64 ? make_work_f64(N, q) : make_work_f32(N, q);
+        const std::vector<Params> ps{q};
+        const std::vector<int64_t> ns{N};
+        WorkI *w = dtype == SPH_F64 ? make_work_f64(ps, ns) : make_work_f32(ps, ns);
         *out = reinterpret_cast<sph_workspace>(w);
     });
 }
@@ -423,11 +427,13 @@ SPH_API int32_t sph_backward(sph_workspace ws, sph_tape tp, sph_field theta, con
         need(ws, "workspace");
         need(tp, "tape");
         need(theta, "theta");
-        const Params q = to_params(p);
+        Params q;
+        if (p) q = to_params(p);
         NLOpts o{skin, interval, maxnb};
         if (o.interval < 1 || o.maxnb < 1) throw Error(ERR_ARG, "interval and maxnb must be positive");
         uint32_t f = 0;
-        WS(ws)->backward(TP(tp), FD(theta), &q, seedX, seedV, scratch ? ST(scratch) : nullptr, o, &f);
+        WS(ws)->backward(TP(tp), FD(theta), p ? &q : nullptr, seedX, seedV,
+                         scratch ? ST(scratch) : nullptr, o, &f);
         if (flags) *flags = f;
     });
 }
@@ -449,7 +455,9 @@ SPH_API int32_t sph_objective(sph_workspace ws, sph_state st, int32_t kind, cons
         need(st, "state");
         Params q;
         if (p) q = to_params(p);
-        const double j = WS(ws)->objective(ST(st), kind, args, p ? &q : nullptr);
+        if (WS(ws)->batch() != 1) throw Error(ERR_ARG, "use sph_batch_objective for a batch");
+        double j = 0.0;
+        WS(ws)->objective(ST(st), kind, args, p ? &q : nullptr, &j);
         if (J) *J = j;
     });
 }
@@ -462,12 +470,101 @@ SPH_API int32_t sph_backward_seeded(sph_workspace ws, sph_tape tp, sph_field the
         need(ws, "workspace");
         need(tp, "tape");
         need(theta, "theta");
-        const Params q = to_params(p);
+        Params q;
+        if (p) q = to_params(p);
         NLOpts o{skin, interval, maxnb};
         if (o.interval < 1 || o.maxnb < 1) throw Error(ERR_ARG, "interval and maxnb must be positive");
         uint32_t f = 0;
-        WS(ws)->backward_seeded(TP(tp), FD(theta), &q, scratch ? ST(scratch) : nullptr, o, &f);
+        WS(ws)->backward_seeded(TP(tp), FD(theta), p ? &q : nullptr,
+                                scratch ? ST(scratch) : nullptr, o, &f);
         if (flags) *flags = f;
+    });
+}
+
+// ---- batches: B independent instances packed into one State/field/workspace ----
+static void batch_specs(int32_t B, const sph_params *params, const int64_t *N,
+                        std::vector<Params> &ps, std::vector<int64_t> &ns)
+{
+    if (B < 1) throw Error(ERR_ARG, "batch size must be >= 1");
+    need(params, "params");
+    need(N, "N");
+    for (int32_t b = 0; b < B; ++b) {
+        ps.push_back(to_params(params + b));
+        ns.push_back(N[b]);
+    }
+}
+
+SPH_API int32_t sph_batch_create(int32_t B, const sph_params *params, const int64_t *N,
+                                 const void *X0, const void *V0, int32_t dtype, double skin,
+                                 int32_t interval, int32_t maxnb, sph_state *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        std::vector<Params> ps;
+        std::vector<int64_t> ns;
+        batch_specs(B, params, N, ps, ns);
+        NLOpts o{skin, interval, maxnb};
+        StateI *s = dtype == SPH_F64 ? make_state_f64(ps, ns, X0, V0, o)
+                                     : make_state_f32(ps, ns, X0, V0, o);
+        *out = reinterpret_cast<sph_state>(s);
+    });
+}
+
+SPH_API int32_t sph_batch_field_create(int32_t B, const int32_t *ngx, const int32_t *ngy,
+                                       int32_t dtype, const void *theta, sph_field *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        need(ngx, "ngx");
+        need(ngy, "ngy");
+        check_dtype(dtype);
+        if (B < 1) throw Error(ERR_ARG, "batch size must be >= 1");
+        const std::vector<int> gx(ngx, ngx + B), gy(ngy, ngy + B);
+        FieldI *f = dtype == SPH_F64 ? make_field_f64(gx, gy, theta) : make_field_f32(gx, gy, theta);
+        *out = reinterpret_cast<sph_field>(f);
+    });
+}
+
+SPH_API int32_t sph_batch_workspace_create(int32_t B, const sph_params *params, const int64_t *N,
+                                           int32_t dtype, sph_workspace *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        check_dtype(dtype);
+        std::vector<Params> ps;
+        std::vector<int64_t> ns;
+        batch_specs(B, params, N, ps, ns);
+        WorkI *w = dtype == SPH_F64 ? make_work_f64(ps, ns) : make_work_f32(ps, ns);
+        *out = reinterpret_cast<sph_workspace>(w);
+    });
+}
+
+SPH_API int32_t sph_batch_size(sph_state st, int32_t *B)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(B, "B");
+        *B = ST(st)->batch();
+    });
+}
+
+SPH_API int32_t sph_batch_take_flags(sph_state st, uint32_t *flags)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(flags, "flags");
+        ST(st)->take_flags_batch(flags);
+    });
+}
+
+SPH_API int32_t sph_batch_objective(sph_workspace ws, sph_state st, int32_t kind,
+                                    const double *args, double *J)
+{
+    return guarded([&] {
+        need(ws, "workspace");
+        need(st, "state");
+        WS(ws)->objective(ST(st), kind, args, nullptr, J);
     });
 }
 

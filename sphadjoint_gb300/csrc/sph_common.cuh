@@ -53,19 +53,56 @@ template <typename T> struct Phys {
     T hxg, hyg, ngx1, ngy1, gxmax, gymax;
 };
 
-// Everything a neighbour loop needs about the particle system: positions in
-// cell order, the neighbour masks and the cell table of the last rebuild.
-template <typename T> struct NLView {
-    int64_t N;
-    int nx, ny;
+// Per-instance constants. A State is one instance; a batch packs B instances
+// (uneven particle counts, their own parameters, cell grids and design
+// fields) into the same arrays: instance b owns particle slots/ids
+// [off, off + n), cells [coff, coff + nx*ny) of the packed cell table and
+// design nodes [toff, toff + ngx*ngy). Sorting by packed cell index keeps
+// every instance in its own slot range, so one cell-list build serves all.
+template <typename T> struct Inst {
+    Phys<T> p;
+    int off, n;       // particle range
+    int nx, ny, coff; // cell grid and its offset in the packed cell table
+    int toff;         // design-node offset
     int maxnb;
-    T rc2, r2min;
+    int lgN;          // ceil(log2(n + 1)), for the exact dJ/dtheta scale
+    T cs, invcs, rc2, r2min, dmax2;
+};
+
+// Arrays shared by all instances (cell order), plus the instance table.
+template <typename T> struct NLView {
+    int64_t N; // total particles
     const T2<T> *pos;
     const T2<T> *xref;
-    const uint32_t *center;   // cx | cy << 16 | spill << 31 (1-based cx, cy)
+    const uint32_t *center;   // cx | cy << 16 | spill << 31 (1-based, instance grid)
     const uint64_t *masks;    // 3 rows, slot-major: masks[r * N + i]
-    const int32_t *cellStart; // ncell + 1 exclusive offsets
+    const int32_t *cellStart; // packed table, total cells + 1 exclusive offsets
+    const Inst<T> *inst;      // instance table
+    const uint16_t *pinst;    // instance of each slot (nullptr: one instance)
+    Inst<T> one;              // the instance itself when there is only one
 };
+
+template <typename T> __device__ __forceinline__ int inst_of(const NLView<T> &v, int64_t i)
+{
+    return v.pinst ? (int)v.pinst[i] : 0;
+}
+
+// Instance constants of slot i: from the kernel parameters when the system
+// holds one instance (constant bank, no memory traffic), from the table
+// otherwise. Copied by value so only the fields a kernel uses are loaded.
+template <bool MULTI, typename T>
+__device__ __forceinline__ decltype(auto) load_inst(const NLView<T> &v, int64_t i)
+{
+    if constexpr (MULTI) return (v.inst[v.pinst[i]]); // const Inst<T>& into the table
+    else return Inst<T>(v.one);                       // value from the parameters
+}
+
+template <bool MULTI, typename T>
+__device__ __forceinline__ decltype(auto) pick_inst(const Inst<T> &one, const Inst<T> *inst, int b)
+{
+    if constexpr (MULTI) return (inst[b]);
+    else return Inst<T>(one);
+}
 
 // Visit the neighbours of particle i in the reference's scan order
 // (src/neighbors.jl:217-244): cell rows ddy = -1..1, within a row cells
@@ -77,7 +114,8 @@ template <typename T> struct NLView {
 // rebuild positions and truncates at maxnb, which is exactly what the
 // reference's fixed-length neighbour rows hold.
 template <typename T, typename F>
-__device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, int64_t i, F &&f)
+__device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, const Inst<T> &I, int64_t i,
+                                                  F &&f)
 {
     const uint32_t cc = v.center[i];
     const int cx = (int)(cc & 0xffffu);
@@ -90,13 +128,13 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, int64_t i,
         // that runs out of bits in one word moves to its next word while the
         // others keep visiting neighbours, so a warp pays for its largest
         // total neighbour count rather than the sum of its per-row maxima.
-        const int row0 = (jx0 - 1) + (cy - 2) * v.nx; // cell (jx0, cy - 1), 0-based
+        const int row0 = I.coff + (jx0 - 1) + (cy - 2) * I.nx; // cell (jx0, cy - 1)
         const uint64_t m0 = v.masks[i];
         const uint64_t m1 = v.masks[v.N + i];
         const uint64_t m2 = v.masks[2 * v.N + i];
         const int b0 = m0 ? v.cellStart[row0] : 0;
-        const int b1 = m1 ? v.cellStart[row0 + v.nx] : 0;
-        const int b2 = m2 ? v.cellStart[row0 + 2 * v.nx] : 0;
+        const int b1 = m1 ? v.cellStart[row0 + I.nx] : 0;
+        const int b2 = m2 ? v.cellStart[row0 + 2 * I.nx] : 0;
         uint32_t m = (uint32_t)m0;
         int base = b0;
         int w = 0;
@@ -114,20 +152,20 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, int64_t i,
             f(base + k);
         }
     } else {
-        const int jx1 = cx + 1 < v.nx ? cx + 1 : v.nx;
+        const int jx1 = cx + 1 < I.nx ? cx + 1 : I.nx;
         const T2<T> xr = v.xref[i];
         int cnt = 0;
         for (int r = 0; r < 3; ++r) {
             const int jy = cy + r - 1;
-            if (jy < 1 || jy > v.ny) continue;
-            const int64_t row = (int64_t)(jy - 1) * v.nx;
-            const int64_t b = v.cellStart[row + jx0 - 1];
-            const int64_t e = v.cellStart[row + jx1];
-            for (int64_t j = b; j < e; ++j) {
+            if (jy < 1 || jy > I.ny) continue;
+            const int row = I.coff + (jy - 1) * I.nx;
+            const int b = v.cellStart[row + jx0 - 1];
+            const int e = v.cellStart[row + jx1];
+            for (int j = b; j < e; ++j) {
                 const T2<T> xj = v.xref[j];
                 const T r2 = r2_exact<T>(sub_rn(xr.x, xj.x), sub_rn(xr.y, xj.y));
-                if (v.r2min < r2 && r2 < v.rc2) {
-                    if (cnt < v.maxnb) {
+                if (I.r2min < r2 && r2 < I.rc2) {
+                    if (cnt < I.maxnb) {
                         ++cnt;
                         f(j);
                     }

@@ -131,16 +131,30 @@ inline void scan_excl(const int32_t *in, int64_t n, int32_t *out, int32_t *out2,
     rt_after_launch(K_SCAN);
 }
 
+// The design field theta of one instance, or the packed fields of a batch
+// (instance b's (ngy, ngx) column-major block at node offset off[b]).
 template <typename T> class Field final : public FieldI {
   public:
-    int nx_, ny_;
+    std::vector<int> gx, gy;
+    std::vector<int64_t> off;
+    int nx_, ny_; // shape of instance 0
     DevBuf<T> th;
-    DevBuf<double> stage;
-    Field(int ngx, int ngy, const void *host) : nx_(ngx), ny_(ngy), th((size_t)ngx * ngy)
+    Field(const std::vector<int> &ngx, const std::vector<int> &ngy, const void *host)
+        : gx(ngx), gy(ngy)
     {
-        if (ngx < 2 || ngy < 2) throw Error(ERR_ARG, "theta must be at least 2 x 2");
+        if (gx.empty() || gx.size() != gy.size()) throw Error(ERR_ARG, "empty theta batch");
+        int64_t tot = 0;
+        for (size_t b = 0; b < gx.size(); ++b) {
+            if (gx[b] < 2 || gy[b] < 2) throw Error(ERR_ARG, "theta must be at least 2 x 2");
+            off.push_back(tot);
+            tot += (int64_t)gx[b] * gy[b];
+        }
+        nx_ = gx[0];
+        ny_ = gy[0];
+        th.alloc((size_t)tot);
         if (host) upload(host); else th.zero();
     }
+    int batch() const { return (int)gx.size(); }
     int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
     int ngx() const override { return nx_; }
     int ngy() const override { return ny_; }
@@ -169,14 +183,19 @@ template <typename T> struct Snap {
 
 template <typename T> class Sys final : public StateI {
   public:
-    Params prm;
+    Params prm;                 // parameters of instance 0 (the State's p)
+    std::vector<Params> prms;   // per instance
+    std::vector<Inst<T>> hinst; // instance table (host copy)
+    DevBuf<Inst<T>> dinst;      // instance table (device)
+    DevBuf<uint16_t> pinst;     // instance of each slot (batches only)
+    int B = 1;
     int64_t N_;
-    int nx, ny;
-    int64_t ncell;
-    double cs_d, rc_d, dmax_d;
+    int nx, ny;                 // grid of instance 0
+    int64_t ncell;              // cells of all instances
+    int64_t nnode = 0;          // design nodes of all instances
+    double cs_d, rc_d, dmax_d;  // instance 0
     NLOpts opts;
     int64_t age = INT64_MAX;
-    T cs, invcs, rc2, r2min, dmax2;
     DevBuf<T2<T>> pos[2], vel[2];
     int cur = 0;
     DevBuf<T2<T>> xref;
@@ -195,31 +214,91 @@ template <typename T> class Sys final : public StateI {
     bool keepAccel = false;
 
     Sys(const Params &p, int64_t N, const void *X0, const void *V0, NLOpts o)
-        : prm(p), N_(N), opts(o)
+        : Sys(std::vector<Params>{p}, std::vector<int64_t>{N}, X0, V0, o)
+    {
+    }
+
+    // NeighborList / CellList constants of one instance (src/neighbors.jl:28-36,
+    // 174-190): rc = Float64(support(p)) * (1 + skin), cs = rc, nx =
+    // ceil(Lx / cs) + 2, dmax = Float64(h) * skin, r2min = eps(T) h h.
+    static Inst<T> make_inst(const Params &p, const NLOpts &o, int64_t off, int64_t n,
+                             int64_t coff, int64_t toff)
     {
         check_params(p);
-        if (N < 0 || N > (int64_t)INT32_MAX - 1) throw Error(ERR_ARG, "particle count out of range");
-        if (o.maxnb < 1) throw Error(ERR_ARG, "maxnb must be positive");
-        if (o.interval < 1) throw Error(ERR_ARG, "interval must be positive");
-        // NeighborList: rc = Float64(support(p)) * (1 + skin), dmax = Float64(h) * skin
+        Inst<T> I;
+        std::memset(&I, 0, sizeof(I));
+        I.p = make_phys<T>(p);
         const T hT = (T)p.h;
         const T support = (T)2 * hT;
-        rc_d = (double)support * (1.0 + o.skin);
-        dmax_d = (double)hT * o.skin;
-        // CellList(backend, N, p; cs = nl.rc)
-        cs_d = rc_d;
+        const double rc = (double)support * (1.0 + o.skin);
+        const double dmax = (double)hT * o.skin;
         const double LxT = (double)(T)p.Lx, LyT = (double)(T)p.Ly;
-        nx = (int)std::max(1.0, std::ceil(LxT / cs_d) + 2);
-        ny = (int)std::max(1.0, std::ceil(LyT / cs_d) + 2);
-        if (!(cs_d > 0) || nx > 65535 || ny > 32767)
+        const double nxd = std::max(1.0, std::ceil(LxT / rc) + 2);
+        const double nyd = std::max(1.0, std::ceil(LyT / rc) + 2);
+        if (!(rc > 0) || !(nxd <= 65535) || !(nyd <= 32767))
             throw Error(ERR_ARG, "cell grid too large (nx <= 65535, ny <= 32767)");
-        ncell = (int64_t)nx * ny;
-        cs = (T)cs_d;
-        invcs = (T)1 / cs;
-        rc2 = (T)(rc_d * rc_d);
-        r2min = std::numeric_limits<T>::epsilon() * hT * hT;
-        dmax2 = (T)(dmax_d * dmax_d);
+        I.off = (int)off;
+        I.n = (int)n;
+        I.nx = (int)nxd;
+        I.ny = (int)nyd;
+        I.coff = (int)coff;
+        I.toff = (int)toff;
+        I.maxnb = o.maxnb;
+        int lg = 0;
+        while (((int64_t)1 << lg) < n + 1 && lg < 62) ++lg;
+        I.lgN = lg;
+        I.cs = (T)rc;
+        I.invcs = (T)1 / I.cs;
+        I.rc2 = (T)(rc * rc);
+        I.r2min = std::numeric_limits<T>::epsilon() * hT * hT;
+        I.dmax2 = (T)(dmax * dmax);
+        return I;
+    }
+
+    Sys(const std::vector<Params> &ps, const std::vector<int64_t> &ns, const void *X0,
+        const void *V0, NLOpts o)
+        : prm(ps.at(0)), prms(ps), N_(0), opts(o)
+    {
+        if (ps.empty() || ps.size() != ns.size()) throw Error(ERR_ARG, "empty instance list");
+        if (ps.size() > 65535) throw Error(ERR_ARG, "at most 65535 instances per batch");
+        if (o.maxnb < 1) throw Error(ERR_ARG, "maxnb must be positive");
+        if (o.interval < 1) throw Error(ERR_ARG, "interval must be positive");
+        B = (int)ps.size();
+        int64_t off = 0, coff = 0, toff = 0;
+        for (int b = 0; b < B; ++b) {
+            if (ns[b] < 0) throw Error(ERR_ARG, "particle count out of range");
+            Inst<T> I = make_inst(ps[b], o, off, ns[b], coff, toff);
+            hinst.push_back(I);
+            off += ns[b];
+            coff += (int64_t)I.nx * I.ny;
+            toff += (int64_t)ps[b].ngx * ps[b].ngy;
+            if (off > (int64_t)INT32_MAX - 1 || coff > (int64_t)INT32_MAX - 1 ||
+                toff > (int64_t)INT32_MAX - 1)
+                throw Error(ERR_ARG, "batch too large for 32-bit slot, cell or node indices");
+        }
+        N_ = off;
+        ncell = coff;
+        nnode = toff;
+        nx = hinst[0].nx;
+        ny = hinst[0].ny;
+        {
+            const T hT = (T)prm.h;
+            rc_d = (double)((T)2 * hT) * (1.0 + o.skin);
+            cs_d = rc_d;
+            dmax_d = (double)hT * o.skin;
+        }
+        dinst.alloc((size_t)B);
+        upload_inst();
+        const int64_t N = N_;
         const size_t n1 = (size_t)std::max<int64_t>(N, 1);
+        if (B > 1) {
+            std::vector<uint16_t> pi(n1, 0);
+            for (int b = 0; b < B; ++b)
+                for (int64_t k = 0; k < ns[b]; ++k) pi[hinst[b].off + k] = (uint16_t)b;
+            pinst.alloc(n1);
+            SPH_CK(cudaMemcpyAsync(pinst.p, pi.data(), sizeof(uint16_t) * n1, cudaMemcpyHostToDevice, rt_stream()));
+            SPH_CK(cudaStreamSynchronize(rt_stream()));
+        }
         for (int k = 0; k < 2; ++k) {
             pos[k].alloc(n1);
             vel[k].alloc(n1);
@@ -236,7 +315,7 @@ template <typename T> class Sys final : public StateI {
         bucketId.alloc(n1);
         scanTmp.alloc((size_t)((ncell + kScanTile - 1) / kScanTile + 1));
         center.alloc(n1);
-        flags.alloc(1);
+        flags.alloc((size_t)B);
         masks.alloc(3 * n1);
         rho.alloc(n1);
         prho.alloc(n1);
@@ -257,6 +336,30 @@ template <typename T> class Sys final : public StateI {
 
     int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
     int64_t N() const override { return N_; }
+    int batch() const override { return B; }
+
+    void upload_inst()
+    {
+        SPH_CK(cudaMemcpyAsync(dinst.p, hinst.data(), sizeof(Inst<T>) * B, cudaMemcpyHostToDevice, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+    }
+
+    // A call may pass its own SPHParams (the reference's kernels take p per
+    // call): the physics constants follow it, the grid and neighbour-list
+    // constants stay those of construction, as in the reference.
+    void use_params(const Params *p)
+    {
+        if (!p) return;
+        if (B != 1) throw Error(ERR_ARG, "a batch uses its per-instance parameters (pass NULL)");
+        check_params(*p);
+        if (std::memcmp(p, &prm, sizeof(Params)) == 0) return;
+        if (p->ngx != prm.ngx || p->ngy != prm.ngy)
+            throw Error(ERR_ARG, "params (ngx, ngy) differ from the state's");
+        prm = *p;
+        prms[0] = *p;
+        hinst[0].p = make_phys<T>(*p);
+        upload_inst();
+    }
 
     void init_identity()
     {
@@ -273,16 +376,14 @@ template <typename T> class Sys final : public StateI {
     {
         NLView<T> v;
         v.N = N_;
-        v.nx = nx;
-        v.ny = ny;
-        v.maxnb = opts.maxnb;
-        v.rc2 = rc2;
-        v.r2min = r2min;
         v.pos = pos[cur].p;
         v.xref = xref.p;
         v.center = center.p;
         v.masks = masks.p;
         v.cellStart = cellStart.p;
+        v.inst = dinst.p;
+        v.pinst = pinst.p;
+        v.one = hinst[0];
         return v;
     }
 
@@ -369,7 +470,8 @@ template <typename T> class Sys final : public StateI {
         const int check = age != INT64_MAX ? 1 : 0;
         if (N_ > 0) {
             counts.zero();
-            SPH_LAUNCH(K_ASSIGN, k_assign<T>, N_, N_, pos[cur].p, xref.p, check, dmax2, cs, nx, ny,
+            auto ka = B > 1 ? &k_assign<T, true> : &k_assign<T, false>;
+            SPH_LAUNCH(K_ASSIGN, ka, N_, N_, pos[cur].p, xref.p, check, hinst[0], dinst.p, pinst.p,
                        cellTmp.p, counts.p, flags.p);
             scan_excl(counts.p, ncell, cellStart.p, cursor.p, scanTmp.p);
             SPH_LAUNCH(K_BUCKET, k_bucket, N_, N_, cellTmp.p, perm.p, cursor.p, bucketSrc.p, bucketId.p);
@@ -378,8 +480,9 @@ template <typename T> class Sys final : public StateI {
                        bucketId.p, pos[cur].p, vel[cur].p, pos[nxt].p, vel[nxt].p, xref.p, perm.p,
                        invperm.p, ex0, ex0N, ex1, ex1N);
             cur = nxt;
-            SPH_LAUNCH(K_NLBUILD, k_nl_build<T>, N_, N_, nx, ny, opts.maxnb, invcs, rc2, r2min,
-                       pos[cur].p, cellStart.p, center.p, masks.p, nbcount.p, flags.p);
+            auto kn = B > 1 ? &k_nl_build<T, true> : &k_nl_build<T, false>;
+            SPH_LAUNCH(K_NLBUILD, kn, N_, N_, hinst[0], dinst.p, pinst.p, pos[cur].p, cellStart.p,
+                       center.p, masks.p, nbcount.p, flags.p);
         }
         age = 0;
         cellsOnlyLatest = false;
@@ -401,7 +504,8 @@ template <typename T> class Sys final : public StateI {
         }
         if (N_ > 0) {
             counts.zero();
-            SPH_LAUNCH(K_ASSIGN, k_assign<T>, N_, N_, pos[cur].p, xref.p, 0, dmax2, cs, nx, ny,
+            auto ka = B > 1 ? &k_assign<T, true> : &k_assign<T, false>;
+            SPH_LAUNCH(K_ASSIGN, ka, N_, N_, pos[cur].p, xref.p, 0, hinst[0], dinst.p, pinst.p,
                        cellTmp.p, counts.p, flags.p);
             scan_excl(counts.p, ncell, clStart.p, cursor.p, scanTmp.p);
             SPH_LAUNCH(K_BUCKET, k_bucket, N_, N_, cellTmp.p, perm.p, cursor.p, bucketSrc.p, bucketId.p);
@@ -430,40 +534,40 @@ template <typename T> class Sys final : public StateI {
     }
 
     // step! (src/forward.jl:161-173); tx/tv: optional tape slot (id order)
-    void step_impl(const T *theta, const Phys<T> &p, T2<T> *tx, T2<T> *tv)
+    void step_impl(const T *theta, T2<T> *tx, T2<T> *tv)
     {
         maybe_rebuild();
         if (N_ == 0) return;
         if (tx) SPH_LAUNCH(K_TAPE, k_tape_store<T>, N_, N_, perm.p, pos[cur].p, vel[cur].p, tx, tv);
         const NLView<T> v = view();
-        SPH_LAUNCH(K_DENSITY, k_density_eos<T>, N_, v, p, rho.p, prho.p);
+        auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
+        SPH_LAUNCH(K_DENSITY, kd, N_, v, rho.p, prho.p);
         const int nxt = 1 - cur;
-        SPH_LAUNCH(K_ACCEL_INTEGRATE, k_accel_integrate<T>, N_, v, p, vel[cur].p, prho.p, theta,
+        auto ki = B > 1 ? &k_accel_integrate<T, true> : &k_accel_integrate<T, false>;
+        SPH_LAUNCH(K_ACCEL_INTEGRATE, ki, N_, v, vel[cur].p, prho.p, theta,
                    pos[nxt].p, vel[nxt].p, keepAccel ? accOut.p : (T2<T> *)nullptr,
                    keepAccel ? alphaOut.p : (T *)nullptr, flags.p);
         cur = nxt;
     }
 
+    // theta must hold one (ngy, ngx) block per instance, in instance order
     Field<T> *field_of(FieldI *f)
     {
         auto *t = dynamic_cast<Field<T> *>(f);
         if (!t) throw Error(ERR_DTYPE, "theta has a different precision than the state");
+        if (t->batch() != B) throw Error(ERR_ARG, "theta has a different number of instances");
+        for (int b = 0; b < B; ++b)
+            if (t->gx[b] != prms[b].ngx || t->gy[b] != prms[b].ngy ||
+                t->off[b] != hinst[b].toff)
+                throw Error(ERR_ARG, "params (ngx, ngy) do not match the theta field");
         return t;
-    }
-
-    static void check_shape(const Params &q, const Field<T> *th)
-    {
-        if (q.ngx != th->nx_ || q.ngy != th->ny_)
-            throw Error(ERR_ARG, "params (ngx, ngy) do not match the theta field");
     }
 
     void step(FieldI *theta, const Params *p) override
     {
+        use_params(p);
         Field<T> *th = field_of(theta);
-        const Params &q = p ? *p : prm;
-        check_params(q);
-        check_shape(q, th);
-        step_impl(th->th.p, make_phys<T>(q), nullptr, nullptr);
+        step_impl(th->th.p, nullptr, nullptr);
         rt_check_launch("step");
     }
 
@@ -471,6 +575,7 @@ template <typename T> class Sys final : public StateI {
 
     void celllist(int32_t *countsOut, int32_t *startsOut, int32_t *orderOut) override
     {
+        if (B != 1) throw Error(ERR_ARG, "cell lists are read per State (batch of one)");
         const int32_t *cst = cellsOnlyLatest ? clStart.p : cellStart.p;
         const int32_t *ord = cellsOnlyLatest ? clOrder.p : perm.p;
         std::vector<int32_t> s((size_t)ncell + 1);
@@ -489,14 +594,22 @@ template <typename T> class Sys final : public StateI {
 
     void neighbors(int32_t *indices, int32_t *nbc) override;
 
-    uint32_t take_flags() override
+    // per-instance flags (read and cleared); returns their union
+    uint32_t take_flags_all(uint32_t *per)
     {
-        uint32_t f = 0;
-        SPH_CK(cudaMemcpyAsync(&f, flags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, rt_stream()));
+        std::vector<uint32_t> f((size_t)B);
+        SPH_CK(cudaMemcpyAsync(f.data(), flags.p, sizeof(uint32_t) * B, cudaMemcpyDeviceToHost, rt_stream()));
         SPH_CK(cudaStreamSynchronize(rt_stream()));
         flags.zero();
-        return f;
+        uint32_t u = 0;
+        for (int b = 0; b < B; ++b) {
+            u |= f[b];
+            if (per) per[b] = f[b];
+        }
+        return u;
     }
+    uint32_t take_flags() override { return take_flags_all(nullptr); }
+    void take_flags_batch(uint32_t *per) override { take_flags_all(per); }
 
     void grid(int32_t *nxo, int32_t *nyo, double *cso, int64_t *ageo) const override
     {
@@ -548,14 +661,37 @@ template <typename T> class Sys final : public StateI {
         center.copy_from(o->center); masks.copy_from(o->masks); flags.copy_from(o->flags);
         rho.copy_from(o->rho); prho.copy_from(o->prho);
         age = o->age;
-        prm = o->prm;
+        if (std::memcmp(hinst.data(), o->hinst.data(), sizeof(Inst<T>) * B) != 0) {
+            prm = o->prm;
+            prms = o->prms;
+            hinst = o->hinst;
+            upload_inst();
+        }
         cellsOnlyLatest = false;
+    }
+
+    void assign_params(const Sys &o)
+    {
+        if (std::memcmp(hinst.data(), o.hinst.data(), sizeof(Inst<T>) * B) != 0) {
+            prm = o.prm;
+            prms = o.prms;
+            hinst = o.hinst;
+            upload_inst();
+        }
     }
 
     bool same_config(const Sys &o) const
     {
-        return N_ == o.N_ && nx == o.nx && ny == o.ny && opts.maxnb == o.opts.maxnb &&
-               opts.interval == o.opts.interval && rc_d == o.rc_d;
+        if (N_ != o.N_ || B != o.B || opts.maxnb != o.opts.maxnb ||
+            opts.interval != o.opts.interval || opts.skin != o.opts.skin)
+            return false;
+        for (int b = 0; b < B; ++b) {
+            const Inst<T> &a = hinst[b], &c = o.hinst[b];
+            if (a.off != c.off || a.n != c.n || a.nx != c.nx || a.ny != c.ny || a.coff != c.coff ||
+                a.toff != c.toff || a.cs != c.cs)
+                return false;
+        }
+        return true;
     }
 };
 
@@ -568,9 +704,10 @@ __global__ void k_list_neighbors(NLView<T> v, const int32_t *__restrict__ perm,
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     const int32_t id = perm[i];
+    const Inst<T> &I = v.inst[inst_of(v, i)];
     int m = 0;
-    for_each_neighbor<T>(v, i, [&](int j) {
-        out[(int64_t)id * v.maxnb + m] = perm[j] + 1;
+    for_each_neighbor<T>(v, I, i, [&](int j) {
+        out[(int64_t)id * I.maxnb + m] = perm[j] + 1;
         ++m;
     });
     nbc[id] = m;
@@ -592,14 +729,15 @@ template <typename T> void Sys<T>::neighbors(int32_t *indices, int32_t *nbc)
 // and the terminal seeds dJ/dX_T, dJ/dV_T in particle-id order.
 // ---------------------------------------------------------------------------
 template <typename T>
-__global__ void k_objective(int64_t N, int kind, const int32_t *__restrict__ perm,
+__global__ void k_objective(int64_t n, int64_t off, int kind, const int32_t *__restrict__ perm,
                             const T2<T> *__restrict__ pos, const T2<T> *__restrict__ vel, T m,
                             T Lx, T a0, T a1, T a2, T2<T> *__restrict__ seedX,
                             T2<T> *__restrict__ seedV, double *__restrict__ partial)
 {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t t = off + k;
     double j = 0.0;
-    if (t < N) {
+    if (k < n) {
         const int32_t id = perm[t];
         const T2<T> x = pos[t], v = vel[t];
         if (kind == OBJ_KE_RIGHT) {
@@ -705,8 +843,12 @@ template <typename T> class Tape final : public TapeI {
         if (s.N_ != N_) throw Error(ERR_ARG, "tape and state particle counts differ");
         if (nsnap_ && recomp && !recomp->same_config(s))
             throw Error(ERR_ARG, "checkpoint tape was bound to a state with another configuration");
-        if (nsnap_ && !recomp)
-            recomp.reset(new Sys<T>(s.prm, s.N_, nullptr, nullptr, s.opts));
+        if (nsnap_ && !recomp) {
+            std::vector<int64_t> ns;
+            for (const auto &I : s.hinst) ns.push_back(I.n);
+            recomp.reset(new Sys<T>(s.prms, ns, nullptr, nullptr, s.opts));
+        }
+        if (nsnap_) recomp->assign_params(s);
     }
 };
 
@@ -714,11 +856,8 @@ template <typename T> class Tape final : public TapeI {
 template <typename T>
 void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tape)
 {
+    use_params(p);
     Field<T> *th = field_of(theta);
-    const Params &q = p ? *p : prm;
-    check_params(q);
-    check_shape(q, th);
-    const Phys<T> ph = make_phys<T>(q);
     Tape<T> *tp = nullptr;
     if (tape) {
         tp = dynamic_cast<Tape<T> *>(tape);
@@ -744,7 +883,7 @@ void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tap
             }
             tp->n_ += 1;
         }
-        step_impl(th->th.p, ph, tx, tv);
+        step_impl(th->th.p, tx, tv);
     }
     SPH_CK(cudaStreamSynchronize(rt_stream()));
     rt_check_launch("simulate");
@@ -756,7 +895,12 @@ void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tap
 template <typename T> class Work final : public WorkI {
   public:
     int64_t N_;
-    int ngx, ngy;
+    int ngx, ngy;                // design grid of instance 0
+    std::vector<Params> prms;    // per instance
+    std::vector<int64_t> ns;     // particles per instance
+    std::vector<int64_t> toffs;  // design-node offset per instance
+    int B = 1;
+    int64_t nnode = 0;
     DevBuf<T2<T>> gX[2], gV[2];
     int gcur = 0;
     DevBuf<T2<T>> abar, gXs, stage2;
@@ -772,9 +916,21 @@ template <typename T> class Work final : public WorkI {
     bool haveResult = false;
     bool haveDevSeeds = false;
 
-    Work(int64_t N, const Params &p) : N_(N), ngx(p.ngx), ngy(p.ngy)
+    Work(int64_t N, const Params &p) : Work(std::vector<Params>{p}, std::vector<int64_t>{N}) {}
+
+    Work(const std::vector<Params> &ps, const std::vector<int64_t> &nsv)
+        : N_(0), ngx(ps.at(0).ngx), ngy(ps.at(0).ngy), prms(ps), ns(nsv)
     {
-        check_params(p);
+        if (ps.empty() || ps.size() != nsv.size()) throw Error(ERR_ARG, "empty instance list");
+        B = (int)ps.size();
+        for (int b = 0; b < B; ++b) {
+            check_params(ps[b]);
+            if (nsv[b] < 0) throw Error(ERR_ARG, "particle count out of range");
+            toffs.push_back(nnode);
+            nnode += (int64_t)ps[b].ngx * ps[b].ngy;
+            N_ += nsv[b];
+        }
+        const int64_t N = N_;
         const size_t n1 = (size_t)std::max<int64_t>(N, 1);
         for (int k = 0; k < 2; ++k) {
             gX[k].alloc(n1);
@@ -784,19 +940,20 @@ template <typename T> class Work final : public WorkI {
         }
         abar.alloc(n1); gXs.alloc(n1); stage2.alloc(n1); outX.alloc(n1); outV.alloc(n1);
         galpha.alloc(n1); grho.alloc(n1);
-        thetaAcc.alloc(2 * (size_t)ngx * ngy);
-        emax.alloc(2);
-        gtheta.alloc((size_t)ngx * ngy);
-        gthetaT.alloc((size_t)ngx * ngy);
+        thetaAcc.alloc(2 * (size_t)nnode);
+        emax.alloc(2 * (size_t)B);
+        gtheta.alloc((size_t)nnode);
+        gthetaT.alloc((size_t)nnode);
         gtheta.zero();
     }
     int dtype() const override { return sizeof(T) == 8 ? F64 : F32; }
     int64_t N() const override { return N_; }
+    int batch() const override { return B; }
 
     // One reverse step at the pre-state held in (sx, sv); srcInv maps particle
     // ids into the source's slots when the source is a recomputed state.
-    void reverse_step(Sys<T> &S, const T *theta, const Phys<T> &p, const T2<T> *sx,
-                      const T2<T> *sv, const int32_t *srcInv, int parity)
+    void reverse_step(Sys<T> &S, const T *theta, const T2<T> *sx, const T2<T> *sv,
+                      const int32_t *srcInv, int parity)
     {
         SPH_LAUNCH(K_GATHER, k_gather_state<T>, N_, N_, S.perm.p, srcInv, sx, sv, S.pos[S.cur].p,
                    S.vel[S.cur].p);
@@ -806,16 +963,20 @@ template <typename T> class Work final : public WorkI {
         if (did) gcur = g2;
         const NLView<T> v = S.view();
         const T2<T> *vel = S.vel[S.cur].p;
-        SPH_LAUNCH(K_DENSITY, k_density_eos<T>, N_, v, p, (T *)nullptr, S.prho.p);
-        SPH_LAUNCH(K_ACCEL_DRAG, k_accel_drag_adj<T>, N_, v, p, vel, S.prho.p, theta, gX[gcur].p,
-                   gV[gcur].p, abar.p, galpha.p, emax.p + parity);
-        SPH_LAUNCH(K_PASS1, k_pass1_design<T>, N_, v, p, vel, S.prho.p, theta, abar.p, galpha.p,
-                   gXs.p, grho.p, gV[gcur].p);
-        SPH_LAUNCH(K_PASS2, k_pass2_axpy<T>, N_, v, p, grho.p, gXs.p, gX[gcur].p, galpha.p,
-                   emax.p + parity, thetaAcc.p);
-        const int64_t nn = (int64_t)ngx * ngy;
-        SPH_LAUNCH(K_THETA_NODE, k_theta_node, nn, nn, N_, thetaAcc.p, emax.p + parity,
-                   emax.p + (1 - parity), gtheta.p);
+        const bool multi = S.B > 1;
+        auto kd = multi ? &k_density_eos<T, true> : &k_density_eos<T, false>;
+        auto ka = multi ? &k_accel_drag_adj<T, true> : &k_accel_drag_adj<T, false>;
+        auto k1 = multi ? &k_pass1_design<T, true> : &k_pass1_design<T, false>;
+        auto k2 = multi ? &k_pass2_axpy<T, true> : &k_pass2_axpy<T, false>;
+        SPH_LAUNCH(K_DENSITY, kd, N_, v, (T *)nullptr, S.prho.p);
+        SPH_LAUNCH(K_ACCEL_DRAG, ka, N_, v, vel, S.prho.p, theta, gX[gcur].p, gV[gcur].p, abar.p,
+                   galpha.p, emax.p, parity);
+        SPH_LAUNCH(K_PASS1, k1, N_, v, vel, S.prho.p, theta, abar.p, galpha.p, gXs.p, grho.p,
+                   gV[gcur].p);
+        SPH_LAUNCH(K_PASS2, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p, parity,
+                   thetaAcc.p);
+        SPH_LAUNCH(K_THETA_NODE, k_theta_node<T>, nnode, nnode, S.B, S.dinst.p, thetaAcc.p, emax.p,
+                   parity, gtheta.p);
     }
 
     void backward(TapeI *tape, FieldI *theta, const Params *p, const void *seedX,
@@ -833,36 +994,48 @@ template <typename T> class Work final : public WorkI {
                       const void *seedV, bool devSeeds, StateI *scratch, NLOpts opts,
                       uint32_t *flags);
 
-    double objective(StateI *sti, int kind, const double *args, const Params *pp) override
+    // J of every instance (J[b]); args: 3 values per instance for the target
+    // objective (xc, yc, sigma), or NULL for the kinetic energy
+    void objective(StateI *sti, int kind, const double *args, const Params *pp,
+                   double *J) override
     {
         auto *st = dynamic_cast<Sys<T> *>(sti);
         if (!st) throw Error(ERR_DTYPE, "state has a different precision than the workspace");
-        if (st->N_ != N_) throw Error(ERR_ARG, "state and workspace particle counts differ");
+        if (st->N_ != N_ || st->B != B) throw Error(ERR_ARG, "state and workspace shapes differ");
         if (kind != OBJ_KE_RIGHT && kind != OBJ_TARGET) throw Error(ERR_ARG, "unknown objective");
         if (kind == OBJ_TARGET && !args) throw Error(ERR_ARG, "target objective needs (xc, yc, sigma)");
-        const Params &q = pp ? *pp : st->prm;
+        st->use_params(pp);
         const size_t n1 = (size_t)std::max<int64_t>(N_, 1);
+        // block partials of every instance, then one J slot per instance
+        int64_t nbTot = 0;
+        for (int b = 0; b < B; ++b) nbTot += grid_for(st->hinst[b].n);
         if (!devSeedX.p) {
             devSeedX.alloc(n1);
             devSeedV.alloc(n1);
-            partial.alloc((size_t)grid_for(std::max<int64_t>(N_, 1)) + 1);
+            partial.alloc((size_t)nbTot + (size_t)B + 1);
         }
-        double J = 0.0;
-        if (N_) {
-            const T a0 = args ? (T)args[0] : (T)0, a1 = args ? (T)args[1] : (T)0,
-                    a2 = args ? (T)args[2] : (T)1;
-            SPH_LAUNCH(K_MISC, k_objective<T>, N_, N_, kind, st->perm.p, st->pos[st->cur].p,
-                       st->vel[st->cur].p, (T)q.m, (T)q.Lx, a0, a1, a2, devSeedX.p, devSeedV.p,
-                       partial.p);
-            const int64_t nb = grid_for(N_);
+        std::vector<double> Jb((size_t)B, 0.0);
+        int64_t pofs = 0;
+        for (int b = 0; b < B; ++b) {
+            const Inst<T> &I = st->hinst[b];
+            if (!I.n) continue;
+            const Params &q = st->prms[b];
+            const T a0 = args ? (T)args[3 * b] : (T)0, a1 = args ? (T)args[3 * b + 1] : (T)0,
+                    a2 = args ? (T)args[3 * b + 2] : (T)1;
+            SPH_LAUNCH(K_MISC, k_objective<T>, (int64_t)I.n, (int64_t)I.n, (int64_t)I.off, kind,
+                       st->perm.p, st->pos[st->cur].p, st->vel[st->cur].p, (T)q.m, (T)q.Lx, a0, a1,
+                       a2, devSeedX.p, devSeedV.p, partial.p + pofs);
+            const int64_t nb = grid_for(I.n);
             rt_before_launch(K_MISC);
-            k_sum_partials<<<1, kBlock, 0, rt_stream()>>>(nb, partial.p, partial.p + nb);
+            k_sum_partials<<<1, kBlock, 0, rt_stream()>>>(nb, partial.p + pofs, partial.p + nbTot + b);
             rt_after_launch(K_MISC);
-            SPH_CK(cudaMemcpyAsync(&J, partial.p + nb, sizeof(double), cudaMemcpyDeviceToHost, rt_stream()));
-            SPH_CK(cudaStreamSynchronize(rt_stream()));
+            pofs += nb;
         }
+        SPH_CK(cudaMemcpyAsync(Jb.data(), partial.p + nbTot, sizeof(double) * B, cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+        for (int b = 0; b < B; ++b)
+            if (J) J[b] = st->hinst[b].n ? Jb[b] : 0.0;
         haveDevSeeds = true;
-        return J;
     }
 
     void get(void *gXo, void *gVo, void *gth) override
@@ -872,7 +1045,7 @@ template <typename T> class Work final : public WorkI {
         if (N_ && gVo) SPH_CK(cudaMemcpyAsync(gVo, outV.p, outV.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
         SPH_CK(cudaStreamSynchronize(rt_stream()));
         if (gth) {
-            const int64_t nn = (int64_t)ngx * ngy;
+            const int64_t nn = nnode;
             SPH_LAUNCH(K_MISC, k_to_T<T>, nn, nn, gtheta.p, gthetaT.p);
             SPH_CK(cudaMemcpyAsync(gth, gthetaT.p, gthetaT.bytes(), cudaMemcpyDeviceToHost, rt_stream()));
             SPH_CK(cudaStreamSynchronize(rt_stream()));
@@ -890,25 +1063,38 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     if (tp->N_ != N_) throw Error(ERR_ARG, "tape and workspace particle counts differ");
     auto *th = dynamic_cast<Field<T> *>(theta);
     if (!th) throw Error(ERR_DTYPE, "theta has a different precision than the workspace");
-    if (th->nx_ != ngx || th->ny_ != ngy) throw Error(ERR_ARG, "theta shape does not match the workspace");
-    if (!pp) throw Error(ERR_ARG, "backward needs the parameters");
-    check_params(*pp);
-    if (pp->ngx != ngx || pp->ngy != ngy)
-        throw Error(ERR_ARG, "params (ngx, ngy) do not match the workspace");
-    const Phys<T> p = make_phys<T>(*pp);
+    if (th->batch() != B) throw Error(ERR_ARG, "theta has a different number of instances");
+    for (int b = 0; b < B; ++b)
+        if (th->gx[b] != prms[b].ngx || th->gy[b] != prms[b].ngy)
+            throw Error(ERR_ARG, "theta shape does not match the workspace");
+    std::vector<Params> ps = prms;
+    if (pp) {
+        if (B != 1) throw Error(ERR_ARG, "a batch uses its per-instance parameters (pass NULL)");
+        check_params(*pp);
+        if (pp->ngx != ngx || pp->ngy != ngy)
+            throw Error(ERR_ARG, "params (ngx, ngy) do not match the workspace");
+        ps[0] = *pp;
+    } else if (B == 1) {
+        throw Error(ERR_ARG, "backward needs the parameters");
+    }
 
     // scratch State (src/driver.jl:153-156): fresh unless the caller passes one
     Sys<T> *S = nullptr;
     if (scratch) {
         S = dynamic_cast<Sys<T> *>(scratch);
         if (!S) throw Error(ERR_DTYPE, "scratch state has a different precision");
-        if (S->N_ != N_) throw Error(ERR_ARG, "scratch state particle count differs");
+        if (S->N_ != N_ || S->B != B) throw Error(ERR_ARG, "scratch state shape differs");
+        if (B == 1) S->use_params(&ps[0]);
     } else {
-        if (!own || own->opts.skin != opts.skin || own->opts.interval != opts.interval ||
-            own->opts.maxnb != opts.maxnb || own->prm.h != pp->h || own->prm.Lx != pp->Lx ||
-            own->prm.Ly != pp->Ly)
-            own.reset(new Sys<T>(*pp, N_, nullptr, nullptr, opts));
+        bool same = own && own->opts.skin == opts.skin && own->opts.interval == opts.interval &&
+                    own->opts.maxnb == opts.maxnb;
+        if (same)
+            for (int b = 0; b < B; ++b)
+                same = same && own->prms[b].h == ps[b].h && own->prms[b].Lx == ps[b].Lx &&
+                       own->prms[b].Ly == ps[b].Ly;
+        if (!same) own.reset(new Sys<T>(ps, ns, nullptr, nullptr, opts));
         S = own.get();
+        if (B == 1) S->use_params(&ps[0]);
         // a fresh State: neighbour list never built, no flags
         S->age = INT64_MAX;
         S->flags.zero();
@@ -936,8 +1122,9 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     gtheta.zero();
     thetaAcc.zero();
     {
-        const int init[2] = {INT_MIN, INT_MIN};
-        SPH_CK(cudaMemcpyAsync(emax.p, init, sizeof(init), cudaMemcpyHostToDevice, rt_stream()));
+        const std::vector<int> init(2 * (size_t)B, INT_MIN);
+        SPH_CK(cudaMemcpyAsync(emax.p, init.data(), sizeof(int) * init.size(), cudaMemcpyHostToDevice, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
     }
 
     const int64_t L = tp->n_;
@@ -945,12 +1132,13 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     tp->fwdSteps = 0;
     if (tp->nsnap_ == 0) {
         for (int64_t n = L - 1; n >= 0; --n) {
-            reverse_step(*S, th->th.p, p, tp->hx.p + (size_t)n * N_, tp->hv.p + (size_t)n * N_,
+            reverse_step(*S, th->th.p, tp->hx.p + (size_t)n * N_, tp->hv.p + (size_t)n * N_,
                          nullptr, (int)(rstep & 1));
             ++rstep;
         }
     } else if (L > 0) {
         Sys<T> &R = *tp->recomp;
+        if (B == 1) R.use_params(&ps[0]);
         // snapshots taken by simulate!, in position order
         std::vector<std::pair<int64_t, int>> taken;
         for (size_t k = 0; k < tp->slotPos.size(); ++k)
@@ -964,12 +1152,12 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
         for (int k = C - 1; k >= 0; --k)
             if (tp->slotPos[k] < 0 || tp->slotPos[k] >= L) freeSlots.push_back(k);
         auto advance = [&](int64_t m) {
-            for (int64_t s = 0; s < m; ++s) R.step_impl(th->th.p, p, nullptr, nullptr);
+            for (int64_t s = 0; s < m; ++s) R.step_impl(th->th.p, nullptr, nullptr);
             tp->fwdSteps += m;
         };
         auto rev_at_R = [&](int64_t n) {
             (void)n;
-            reverse_step(*S, th->th.p, p, R.pos[R.cur].p, R.vel[R.cur].p, R.invperm.p,
+            reverse_step(*S, th->th.p, R.pos[R.cur].p, R.vel[R.cur].p, R.invperm.p,
                          (int)(rstep & 1));
             ++rstep;
         };

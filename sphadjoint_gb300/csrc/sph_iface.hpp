@@ -114,6 +114,8 @@ class StateI {
     virtual void grid(int32_t *nx, int32_t *ny, double *cs, int64_t *age) const = 0;
     virtual void sync() = 0;
     virtual void assign(StateI *src) = 0;
+    virtual int batch() const = 0;
+    virtual void take_flags_batch(uint32_t *per_instance) = 0;
 };
 
 enum ObjectiveKind : int32_t {
@@ -130,19 +132,22 @@ class WorkI {
                           const void *seedV, StateI *scratch, NLOpts opts,
                           uint32_t *flags) = 0;
     virtual void get(void *gX, void *gV, void *gtheta) = 0;
-    // J of the state's current positions/velocities; the terminal seeds stay
-    // on the device for backward_seeded
-    virtual double objective(StateI *st, int kind, const double *args, const Params *p) = 0;
+    virtual int batch() const = 0;
+    // J of each instance's current positions/velocities (J[b]); the terminal
+    // seeds stay on the device for backward_seeded
+    virtual void objective(StateI *st, int kind, const double *args, const Params *p,
+                           double *J) = 0;
     virtual void backward_seeded(TapeI *tape, FieldI *theta, const Params *p, StateI *scratch,
                                  NLOpts opts, uint32_t *flags) = 0;
 };
 
 #define SPH_DECLARE_FACTORIES(SFX)                                                           \
-    FieldI *make_field##SFX(int ngx, int ngy, const void *host);                             \
+    FieldI *make_field##SFX(const std::vector<int> &ngx, const std::vector<int> &ngy,        \
+                            const void *host);                                               \
     TapeI *make_tape##SFX(int64_t N, int64_t cap, int32_t nsnap);                            \
-    StateI *make_state##SFX(const Params &p, int64_t N, const void *X0, const void *V0,      \
-                            NLOpts o);                                                       \
-    WorkI *make_work##SFX(int64_t N, const Params &p);
+    StateI *make_state##SFX(const std::vector<Params> &p, const std::vector<int64_t> &N,     \
+                            const void *X0, const void *V0, NLOpts o);                       \
+    WorkI *make_work##SFX(const std::vector<Params> &p, const std::vector<int64_t> &N);
 
 SPH_DECLARE_FACTORIES(_f32)
 SPH_DECLARE_FACTORIES(_f64)

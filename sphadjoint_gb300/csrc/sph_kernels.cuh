@@ -126,25 +126,30 @@ static __global__ void k_scan_down(const int32_t *__restrict__ in, int64_t n,
 
 // Cell of every particle (division form x / cs as in cell_index), warp-
 // aggregated histogram, and the displacement check of _nl_build!
-// (src/neighbors.jl:207-213) against the previous rebuild positions.
-template <typename T>
+// (src/neighbors.jl:207-213) against the previous rebuild positions. Cells are
+// numbered in the packed table (instance offset + local cell).
+template <typename T, bool MULTI>
 __global__ void k_assign(int64_t N, const T2<T> *__restrict__ pos, const T2<T> *__restrict__ xref,
-                         int check, T dmax2, T cs, int nx, int ny, int32_t *__restrict__ cellTmp,
+                         int check, const Inst<T> one, const Inst<T> *__restrict__ inst,
+                         const uint16_t *__restrict__ pinst, int32_t *__restrict__ cellTmp,
                          int32_t *__restrict__ counts, uint32_t *__restrict__ flags)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < N;
     int32_t c = -1;
     if (live) {
+        const int b = MULTI ? (int)pinst[i] : 0;
+        decltype(auto) I = pick_inst<MULTI>(one, inst, b);
         const T2<T> x = pos[i];
         if (check) {
             const T2<T> xr = xref[i];
             const T d2 = r2_exact<T>(sub_rn(x.x, xr.x), sub_rn(x.y, xr.y));
-            if (d2 > dmax2) atomicOr(flags, FLAG_DISPLACEMENT);
+            if (d2 > I.dmax2) atomicOr(flags + b, FLAG_DISPLACEMENT);
         }
-        const int cx = cell_coord<T>(x.x / cs, nx);
-        const int cy = cell_coord<T>(x.y / cs, ny);
-        c = (cx - 1) + (cy - 1) * nx;
+        const T cs = I.cs;
+        const int cx = cell_coord<T>(x.x / cs, I.nx);
+        const int cy = cell_coord<T>(x.y / cs, I.ny);
+        c = I.coff + (cx - 1) + (cy - 1) * I.nx;
         cellTmp[i] = c;
     }
     const unsigned act = __ballot_sync(0xffffffffu, live);
@@ -157,8 +162,8 @@ __global__ void k_assign(int64_t N, const T2<T> *__restrict__ pos, const T2<T> *
 // Scatter every particle into its cell's bucket (arbitrary order inside the
 // bucket; the rank step below makes it deterministic).
 static __global__ void k_bucket(int64_t N, const int32_t *__restrict__ cellTmp,
-                         const int32_t *__restrict__ perm, int32_t *__restrict__ cursor,
-                         int32_t *__restrict__ bucketSrc, int32_t *__restrict__ bucketId)
+                                const int32_t *__restrict__ perm, int32_t *__restrict__ cursor,
+                                int32_t *__restrict__ bucketSrc, int32_t *__restrict__ bucketId)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < N;
@@ -212,17 +217,22 @@ __global__ void k_rank_permute(int64_t N, const int32_t *__restrict__ cellTmp,
 // _nl_build! (src/neighbors.jl:192-245): the scan centre uses x * invcs as
 // the reference does; a neighbour is kept if r2min < r^2 < rc^2, in scan order,
 // at most maxnb of them (overflow sets the flag, like flags[1]).
-template <typename T>
-__global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2, T r2min,
-                           const T2<T> *__restrict__ pos, const int32_t *__restrict__ cellStart,
-                           uint32_t *__restrict__ center, uint64_t *__restrict__ masks,
-                           int32_t *__restrict__ nbcount, uint32_t *__restrict__ flags)
+template <typename T, bool MULTI>
+__global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restrict__ inst,
+                           const uint16_t *__restrict__ pinst, const T2<T> *__restrict__ pos,
+                           const int32_t *__restrict__ cellStart, uint32_t *__restrict__ center,
+                           uint64_t *__restrict__ masks, int32_t *__restrict__ nbcount,
+                           uint32_t *__restrict__ flags)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
+    const int bi = MULTI ? (int)pinst[i] : 0;
+    decltype(auto) I = pick_inst<MULTI>(one, inst, bi);
+    const int nx = I.nx, ny = I.ny, maxnb = I.maxnb;
+    const T rc2 = I.rc2, r2min = I.r2min;
     const T2<T> xi = pos[i];
-    const int cx = cell_coord<T>(xi.x * invcs, nx);
-    const int cy = cell_coord<T>(xi.y * invcs, ny);
+    const int cx = cell_coord<T>(xi.x * I.invcs, nx);
+    const int cy = cell_coord<T>(xi.y * I.invcs, ny);
     const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
     const int jx1 = cx + 1 < nx ? cx + 1 : nx;
     uint32_t spill = 0;
@@ -233,7 +243,7 @@ __global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2,
         uint32_t lo = 0, hi = 0;
         const int jy = cy + r - 1;
         if (jy >= 1 && jy <= ny) {
-            const int row = (jy - 1) * nx;
+            const int row = I.coff + (jy - 1) * nx;
             const int b = cellStart[row + jx0 - 1];
             const int e = cellStart[row + jx1];
             if (e - b > 64) spill = 1;
@@ -256,7 +266,7 @@ __global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2,
     }
     center[i] = (uint32_t)cx | ((uint32_t)cy << 16) | (spill << 31);
     nbcount[i] = m;
-    if (over) atomicOr(flags, FLAG_NL_OVERFLOW);
+    if (over) atomicOr(flags + bi, FLAG_NL_OVERFLOW);
 }
 
 // ---------------------------------------------------------------------------
@@ -264,59 +274,60 @@ __global__ void k_nl_build(int64_t N, int nx, int ny, int maxnb, T invcs, T rc2,
 // integrate_kernel! (fused; positions and velocities double-buffered because
 // neighbours read the pre-step state).
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_density_eos(NLView<T> v, Phys<T> p,
-                                                        T *__restrict__ rho,
-                                                        T2<T> *__restrict__ prho)
+template <typename T, bool MULTI>
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
+    k_density_eos(const __grid_constant__ NLView<T> v, T *__restrict__ rho, T2<T> *__restrict__ prho)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    decltype(auto) I = load_inst<MULTI>(v, i);
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, A = I.p.A;
     const T2<T> xi = v.pos[i];
     T acc = (T)0;
-    for_each_neighbor<T>(v, i, [&](int j) {
+    for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < p.r2max) {
-            const T q = pair_sqrt(r2) * p.invh;
+        if (r2 < r2max) {
+            const T q = pair_sqrt(r2) * invh;
             const T u = (T)1 - (T)0.5 * q;
             const T u2 = u * u;
-            acc += p.m * (p.A * u2 * u2 * ((T)2 * q + (T)1));
+            acc += m * (A * u2 * u2 * ((T)2 * q + (T)1));
         }
     });
-    const T ri = acc + p.m * p.A;
+    const T ri = acc + m * A;
     if (rho) rho[i] = ri;
     const T inv = (T)1 / ri;
-    prho[i] = mk2<T>(p.c2 * (ri - p.rho0) * inv * inv, inv);
+    prho[i] = mk2<T>(I.p.c2 * (ri - I.p.rho0) * inv * inv, inv);
 }
 
-// Pressure + Morris viscosity + gravity + wall (accel_kernel!) and the semi-
-// implicit Euler update with implicit Brinkman drag (integrate_kernel!).
+// Pressure + Morris viscosity (accel_kernel! pair loop).
 template <typename T>
-__device__ __forceinline__ void accel_sum(const NLView<T> &v, const Phys<T> &p,
+__device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
                                           const T2<T> *__restrict__ vel,
                                           const T2<T> *__restrict__ prho, int64_t i,
                                           const T2<T> &xi, const T2<T> &vi, T &ax, T &ay)
 {
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, twomumass = I.p.twomumass;
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
     ax = (T)0;
     ay = (T)0;
-    for_each_neighbor<T>(v, i, [&](int j) {
+    for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < p.r2max) {
-            const T q = pair_sqrt(r2) * p.invh;
+        if (r2 < r2max) {
+            const T q = pair_sqrt(r2) * invh;
             const T u = (T)1 - (T)0.5 * q;
-            const T F = p.Fc * u * u * u;
+            const T F = Fc * u * u * u;
             const T2<T> pj = prho[j];
-            const T Pij = p.m * (pti + pj.x);
+            const T Pij = m * (pti + pj.x);
             ax -= Pij * F * dx;
             ay -= Pij * F * dy;
-            const T C = p.twomumass * iri * pj.y * F;
+            const T C = twomumass * iri * pj.y * F;
             const T2<T> vj = vel[j];
             ax += C * (vi.x - vj.x);
             ay += C * (vi.y - vj.y);
@@ -324,34 +335,40 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Phys<T> &p,
     });
 }
 
-template <typename T>
+// accel_kernel! (pressure + viscosity + gravity + wall, and alpha) fused with
+// integrate_kernel! (semi-implicit Euler, implicit Brinkman drag).
+template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kBlock)
-    k_accel_integrate(NLView<T> v, Phys<T> p, const T2<T> *__restrict__ vel,
-                      const T2<T> *__restrict__ prho, const T *__restrict__ theta,
-                      T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
-                      T2<T> *__restrict__ aOut, T *__restrict__ alphaOut,
-                      uint32_t *__restrict__ flags)
+    k_accel_integrate(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
+                      const T2<T> *__restrict__ prho,
+                      const T *__restrict__ theta, T2<T> *__restrict__ posOut,
+                      T2<T> *__restrict__ velOut, T2<T> *__restrict__ aOut,
+                      T *__restrict__ alphaOut, uint32_t *__restrict__ flags)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    const int b = MULTI ? inst_of(v, i) : 0;
+    decltype(auto) I = load_inst<MULTI>(v, i);
     const T2<T> xi = v.pos[i];
     const T2<T> vi = vel[i];
     T ax, ay;
-    accel_sum<T>(v, p, vel, prho, i, xi, vi, ax, ay);
-    const T al = interp_alpha_value<T>(theta, xi.x, xi.y, p);
+    accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+    const Phys<T> &p = I.p;
+    const T al = interp_alpha_value<T>(theta + I.toff, xi.x, xi.y, p);
     ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
     ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
     if (aOut) aOut[i] = mk2<T>(ax, ay);
     if (alphaOut) alphaOut[i] = al;
-    const T D = (T)1 / ((T)1 + p.dt * al);
-    const T v1 = (vi.x + p.dt * ax) * D;
-    const T v2 = (vi.y + p.dt * ay) * D;
-    const T x1 = xi.x + p.dt * v1;
-    const T x2 = xi.y + p.dt * v2;
+    const T dt = p.dt;
+    const T D = (T)1 / ((T)1 + dt * al);
+    const T v1 = (vi.x + dt * ax) * D;
+    const T v2 = (vi.y + dt * ay) * D;
+    const T x1 = xi.x + dt * v1;
+    const T x2 = xi.y + dt * v2;
     velOut[i] = mk2<T>(v1, v2);
     posOut[i] = mk2<T>(x1, x2);
     if (!(isfinite(x1) && isfinite(x2) && isfinite(v1) && isfinite(v2)))
-        atomicOr(flags, FLAG_NONFINITE);
+        atomicOr(flags + b, FLAG_NONFINITE);
 }
 
 // Tape slot in particle-id order (_tape_store!, src/driver.jl:73-77).
@@ -417,78 +434,87 @@ __global__ void k_gather_from_ids(int64_t N, const int32_t *__restrict__ perm,
 // ---------------------------------------------------------------------------
 
 // Accel recompute (accel_kernel!, for a_rest and alpha) + _adj_integrate!
-// (gV += dt gX) + _adj_drag! (implicit Brinkman VJP). Also records the
-// largest binary exponent of |galpha| for the exact theta reduction.
-template <typename T>
+// (gV += dt gX) + _adj_drag! (implicit Brinkman VJP). Also records, per
+// instance, the largest binary exponent of |galpha| for the exact theta
+// reduction (emax holds two slots per instance, selected by step parity).
+template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kBlock)
-    k_accel_drag_adj(NLView<T> v, Phys<T> p, const T2<T> *__restrict__ vel,
-                     const T2<T> *__restrict__ prho, const T *__restrict__ theta,
-                     const T2<T> *__restrict__ gX, T2<T> *__restrict__ gV,
-                     T2<T> *__restrict__ abar, T *__restrict__ galpha,
-                     int *__restrict__ emax)
+    k_accel_drag_adj(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
+                     const T2<T> *__restrict__ prho,
+                     const T *__restrict__ theta, const T2<T> *__restrict__ gX,
+                     T2<T> *__restrict__ gV, T2<T> *__restrict__ abar, T *__restrict__ galpha,
+                     int *__restrict__ emax, int parity)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < v.N;
     int e = INT_MIN;
-    if (i < v.N) {
+    int b = 0;
+    if (live) {
+        b = MULTI ? inst_of(v, i) : 0;
+        decltype(auto) I = load_inst<MULTI>(v, i);
         const T2<T> xi = v.pos[i];
         const T2<T> vi = vel[i];
         T ax, ay;
-        accel_sum<T>(v, p, vel, prho, i, xi, vi, ax, ay);
-        const T al = interp_alpha_value<T>(theta, xi.x, xi.y, p);
+        accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+        const Phys<T> &p = I.p;
+        const T al = interp_alpha_value<T>(theta + I.toff, xi.x, xi.y, p);
         ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
         ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
+        const T dt = p.dt;
         const T2<T> gx = gX[i];
         T2<T> gv = gV[i];
-        gv.x += p.dt * gx.x;
-        gv.y += p.dt * gx.y;
-        const T D = (T)1 / ((T)1 + p.dt * al);
-        const T vx = (vi.x + p.dt * ax) * D;
-        const T vy = (vi.y + p.dt * ay) * D;
-        abar[i] = mk2<T>(p.dt * D * gv.x, p.dt * D * gv.y);
-        const T ga = -p.dt * D * (vx * gv.x + vy * gv.y);
+        gv.x += dt * gx.x;
+        gv.y += dt * gx.y;
+        const T D = (T)1 / ((T)1 + dt * al);
+        const T vx = (vi.x + dt * ax) * D;
+        const T vy = (vi.y + dt * ay) * D;
+        abar[i] = mk2<T>(dt * D * gv.x, dt * D * gv.y);
+        const T ga = -dt * D * (vx * gv.x + vy * gv.y);
         galpha[i] = ga;
         gV[i] = mk2<T>(D * gv.x, D * gv.y);
         if (ga != (T)0 && isfinite(ga)) e = ilogb((double)ga) + 1; // |ga| < 2^e
     }
-    // block max, then one atomic per block
-    for (int o = 16; o > 0; o >>= 1) {
-        const int y = __shfl_xor_sync(0xffffffffu, e, o);
-        e = y > e ? y : e;
+    // max over the lanes of each instance present in the warp, one atomic each
+    const unsigned act = __ballot_sync(0xffffffffu, live);
+    if (!live) return;
+    const unsigned peers = __match_any_sync(act, b);
+    int mx = e;
+    for (unsigned rest = peers; rest; rest &= rest - 1) {
+        const int src = __ffs(rest) - 1;
+        const int y = __shfl_sync(peers, e, src);
+        mx = y > mx ? y : mx;
     }
-    __shared__ int sm[kBlock / 32];
-    if (lane_id() == 0) sm[threadIdx.x >> 5] = e;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int b = sm[0];
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) b = sm[w] > b ? sm[w] : b;
-        if (b != INT_MIN) atomicMax(emax, b);
-    }
+    if ((int)lane_id() == __ffs(peers) - 1 && mx != INT_MIN) atomicMax(emax + 2 * b + parity, mx);
 }
 
 // adj_pass1_kernel! (src/adjoint.jl:30-122) + the per-particle half of
 // adj_design_kernel! (gXs += galpha * grad alpha, src/adjoint.jl:173-175)
 // + _axpy2!(gV, gVs).
-template <typename T>
+template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kBlock)
-    k_pass1_design(NLView<T> v, Phys<T> p, const T2<T> *__restrict__ vel,
-                   const T2<T> *__restrict__ prho, const T *__restrict__ theta,
-                   const T2<T> *__restrict__ abar, const T *__restrict__ galpha,
-                   T2<T> *__restrict__ gXs, T *__restrict__ grho, T2<T> *__restrict__ gV)
+    k_pass1_design(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
+                   const T2<T> *__restrict__ prho,
+                   const T *__restrict__ theta, const T2<T> *__restrict__ abar,
+                   const T *__restrict__ galpha, T2<T> *__restrict__ gXs, T *__restrict__ grho,
+                   T2<T> *__restrict__ gV)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    decltype(auto) I = load_inst<MULTI>(v, i);
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc,
+            twomumass = I.p.twomumass;
     const T2<T> xi = v.pos[i];
     const T2<T> vi = vel[i];
     const T2<T> ab = abar[i];
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
     T gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
-    for_each_neighbor<T>(v, i, [&](int j) {
+    for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < p.r2max) {
+        if (r2 < r2max) {
             T r, rinv;
             if constexpr (sizeof(T) == 4) {
                 rinv = r2 > (T)0 ? rsqrtf(r2) : (T)0;
@@ -496,13 +522,13 @@ __global__ void __launch_bounds__(kBlock)
             } else {
                 r = sqrt(r2);
             }
-            const T q = r * p.invh;
+            const T q = r * invh;
             const T u = (T)1 - (T)0.5 * q;
-            const T F = p.Fc * u * u * u;
-            const T G = p.Gc * u * u;
+            const T F = Fc * u * u * u;
+            const T G = Gc * u * u;
             const T2<T> pj = prho[j];
-            const T Pij = p.m * (pti + pj.x);
-            const T Cbase = p.twomumass * iri * pj.y;
+            const T Pij = m * (pti + pj.x);
+            const T Cbase = twomumass * iri * pj.y;
             const T C = Cbase * F;
             const T2<T> abj = abar[j];
             const T2<T> vj = vel[j];
@@ -516,8 +542,8 @@ __global__ void __launch_bounds__(kBlock)
             gy -= Pij * F * day;
             const T Fbar = Pij * ad_d + Cbase * ad_v;
             T w;
-            if constexpr (sizeof(T) == 4) w = Fbar * G * p.invh * rinv;
-            else w = Fbar * G * p.invh / r;
+            if constexpr (sizeof(T) == 4) w = Fbar * G * invh * rinv;
+            else w = Fbar * G * invh / r;
             gx += w * dx;
             gy += w * dy;
             gvx += C * dax;
@@ -526,12 +552,13 @@ __global__ void __launch_bounds__(kBlock)
             sumS += F * ad_d;
         }
     });
+    const Phys<T> &p = I.p;
     grh += ((T)(-2) * p.m * pti * iri) * sumS;
     grh += p.c2 * p.m * iri * iri * sumS;
     gx += ab.x * wall_daccel<T>(xi.x, p.Lx, p.kw);
     gy += ab.y * wall_daccel<T>(xi.y, p.Ly, p.kw);
     T al, dadx, dady;
-    interp_alpha<T>(theta, xi.x, xi.y, p, al, dadx, dady);
+    interp_alpha<T>(theta + I.toff, xi.x, xi.y, p, al, dadx, dady);
     const T ga = galpha[i];
     gXs[i] = mk2<T>(gx + ga * dadx, gy + ga * dady);
     grho[i] = grh;
@@ -546,7 +573,7 @@ __global__ void __launch_bounds__(kBlock)
 // which particles arrive. acc[0] = low word, acc[1] = high word.
 __device__ __forceinline__ void fixed_add(unsigned long long *acc, double c, int S)
 {
-    if (c == 0.0) return;
+    if (c == 0.0 || !isfinite(c)) return;
     double a = rint(ldexp(fabs(c), S));
     if (a == 0.0) return;
     const double hid = floor(ldexp(a, -64));
@@ -562,37 +589,38 @@ __device__ __forceinline__ void fixed_add(unsigned long long *acc, double c, int
     if (h) atomicAdd(acc + 1, h);
 }
 
-__host__ __device__ __forceinline__ int theta_scale(int emax, int64_t N)
-{
-    int lg = 0;
-    while (((int64_t)1 << lg) < N + 1 && lg < 62) ++lg;
-    return 124 - emax - lg;
-}
+// Scale 2^S of the fixed-point grid: every contribution of the step is below
+// 2^emax and at most n of them reach one node, so sums stay below 2^124.
+__host__ __device__ __forceinline__ int theta_scale(int emax, int lgN) { return 124 - emax - lgN; }
 
 // adj_pass2_kernel! (src/adjoint.jl:126-156) + _axpy2!(gX, gXs) + the theta
 // write-back of adj_design_kernel! (src/adjoint.jl:177-184), done as an exact
 // deterministic reduction keyed by design node instead of float atomics.
-template <typename T>
+template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kBlock)
-    k_pass2_axpy(NLView<T> v, Phys<T> p, const T *__restrict__ grho,
-                 const T2<T> *__restrict__ gXs, T2<T> *__restrict__ gX,
-                 const T *__restrict__ galpha, const int *__restrict__ emax,
+    k_pass2_axpy(const __grid_constant__ NLView<T> v, const T *__restrict__ grho,
+                 const T2<T> *__restrict__ gXs,
+                 T2<T> *__restrict__ gX, const T *__restrict__ galpha,
+                 const int *__restrict__ emax, int parity,
                  unsigned long long *__restrict__ thetaAcc)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    const int b = MULTI ? inst_of(v, i) : 0;
+    decltype(auto) I = load_inst<MULTI>(v, i);
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc;
     const T2<T> xi = v.pos[i];
     const T gri = grho[i];
     T gx = 0, gy = 0;
-    for_each_neighbor<T>(v, i, [&](int j) {
+    for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < p.r2max) {
-            const T q = pair_sqrt(r2) * p.invh;
+        if (r2 < r2max) {
+            const T q = pair_sqrt(r2) * invh;
             const T u = (T)1 - (T)0.5 * q;
-            const T w = p.m * (p.Fc * u * u * u) * (gri + grho[j]);
+            const T w = m * (Fc * u * u * u) * (gri + grho[j]);
             gx += w * dx;
             gy += w * dy;
         }
@@ -606,41 +634,55 @@ __global__ void __launch_bounds__(kBlock)
     gX[i] = g;
 
     const T ga = galpha[i];
-    const int em = *emax;
+    const int em = emax[2 * b + parity];
     if (ga != (T)0 && em != INT_MIN) {
+        const Phys<T> &p = I.p;
         int i0, j0;
         T fx, fy, ax, ay;
         interp_cell<T>(xi.x, xi.y, p, i0, j0, fx, fy, ax, ay);
-        const int S = theta_scale(em, v.N);
+        const int S = theta_scale(em, I.lgN);
+        unsigned long long *acc = thetaAcc + 2 * (int64_t)I.toff;
         const int64_t l00 = (int64_t)j0 + (int64_t)i0 * p.ngy;
-        fixed_add(thetaAcc + 2 * l00, (double)(ga * ((T)1 - fx) * ((T)1 - fy)), S);
-        fixed_add(thetaAcc + 2 * (l00 + p.ngy), (double)(ga * fx * ((T)1 - fy)), S);
-        fixed_add(thetaAcc + 2 * (l00 + 1), (double)(ga * ((T)1 - fx) * fy), S);
-        fixed_add(thetaAcc + 2 * (l00 + p.ngy + 1), (double)(ga * fx * fy), S);
+        fixed_add(acc + 2 * l00, (double)(ga * ((T)1 - fx) * ((T)1 - fy)), S);
+        fixed_add(acc + 2 * (l00 + p.ngy), (double)(ga * fx * ((T)1 - fy)), S);
+        fixed_add(acc + 2 * (l00 + 1), (double)(ga * ((T)1 - fx) * fy), S);
+        fixed_add(acc + 2 * (l00 + p.ngy + 1), (double)(ga * fx * fy), S);
     }
 }
 
-// Per design node: gtheta += this step's exact sum; clear the accumulator and
-// the exponent slot the next step will use.
-static __global__ void k_theta_node(int64_t nnode, int64_t N, unsigned long long *__restrict__ acc,
-                             const int *__restrict__ emax, int *__restrict__ emaxNext,
-                             double *__restrict__ gtheta)
+// Per design node: gtheta += this step's exact sum; clear the accumulator.
+// Threads n < B also reset the exponent slot the next step will use.
+template <typename T>
+__global__ void k_theta_node(int64_t nnode, int B, const Inst<T> *__restrict__ inst,
+                             unsigned long long *__restrict__ acc, int *__restrict__ emax,
+                             int parity, double *__restrict__ gtheta)
 {
     const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (n == 0) *emaxNext = INT_MIN;
     if (n >= nnode) return;
     unsigned long long lo = acc[2 * n], hi = acc[2 * n + 1];
-    if ((lo | hi) == 0ull) return;
-    acc[2 * n] = 0ull;
-    acc[2 * n + 1] = 0ull;
-    const bool neg = (long long)hi < 0;
-    if (neg) {
-        lo = ~lo + 1ull;
-        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+    const bool any = (lo | hi) != 0ull;
+    int b = 0;
+    if (any) {
+        // instance owning node n (design-node offsets are increasing)
+        int lo_b = 0, hi_b = B - 1;
+        while (lo_b < hi_b) {
+            const int mid = (lo_b + hi_b + 1) >> 1;
+            if (inst[mid].toff <= n) lo_b = mid; else hi_b = mid - 1;
+        }
+        b = lo_b;
+        const int em = emax[2 * b + parity];
+        acc[2 * n] = 0ull;
+        acc[2 * n + 1] = 0ull;
+        const bool neg = (long long)hi < 0;
+        if (neg) {
+            lo = ~lo + 1ull;
+            hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+        }
+        double vv = ldexp((double)hi, 64) + (double)lo;
+        if (neg) vv = -vv;
+        gtheta[n] += ldexp(vv, -theta_scale(em, inst[b].lgN));
     }
-    double vv = ldexp((double)hi, 64) + (double)lo;
-    if (neg) vv = -vv;
-    gtheta[n] += ldexp(vv, -theta_scale(*emax, N));
+    if (n < B) emax[2 * n + (1 - parity)] = INT_MIN;
 }
 
 template <typename T>

@@ -69,6 +69,29 @@ int32_t *scratch_ptr(int dev)
     return g_ptr[dev];
 }
 
+// _cl_assign! for one grid passed by value: cell of every particle (x / cs,
+// as cell_index does) and a warp-aggregated histogram into `counts`.
+template <typename T>
+__global__ void k_na_assign(int64_t N, const T2<T> *__restrict__ pos, T cs, int nx, int ny,
+                            int32_t *__restrict__ cellTmp, int32_t *__restrict__ counts)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < N;
+    int32_t c = -1;
+    if (live) {
+        const T2<T> x = pos[i];
+        const int cx = cell_coord<T>(x.x / cs, nx);
+        const int cy = cell_coord<T>(x.y / cs, ny);
+        c = (cx - 1) + (cy - 1) * nx;
+        cellTmp[i] = c;
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, live);
+    if (live) {
+        const unsigned peers = __match_any_sync(act, c);
+        if ((int)lane_id() == __ffs(peers) - 1) atomicAdd(counts + c, __popc(peers));
+    }
+}
+
 // k_bucket without a permutation: particle i is its own id.
 __global__ void k_na_bucket(int64_t N, const int32_t *__restrict__ cellTmp,
                             int32_t *__restrict__ cursor, int32_t *__restrict__ bucketSrc)
@@ -116,8 +139,8 @@ void build_cells_noalloc(const void *X, int64_t N, double cs, int nx, int ny, in
 
     cuda_check(cudaMemsetAsync(counts, 0, sizeof(int32_t) * ncell, s), "cudaMemsetAsync(counts)");
     if (N > 0) {
-        k_assign<T><<<grid_blocks(N), kBlock, 0, s>>>(N, (const T2<T> *)X, nullptr, 0, (T)0, csT, nx,
-                                                      ny, cellTmp, counts, nullptr);
+        k_na_assign<T><<<grid_blocks(N), kBlock, 0, s>>>(N, (const T2<T> *)X, csT, nx, ny, cellTmp,
+                                                         counts);
     }
     const int64_t nb = (ncell + kScanTile - 1) / kScanTile;
     if (nb <= 1) {
