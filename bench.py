@@ -187,6 +187,101 @@ def run_batched(args):
     print(json.dumps(line))
 
 
+def served_requests(R, rate, seed=4, ntheta=128, n_range=(2000, 200000),
+                    steps_range=(500, 5000), snapshots=32):
+    """Requests of a topology-optimisation line search: N uniform in
+    [2k, 200k] (square jittered lattice, dx = 1e-3), steps uniform in
+    [500, 5000], theta = base 128 x 128 design + step * direction with the step
+    log-uniform in [1e-3, 1e-1]; Poisson arrivals at `rate` per second."""
+    rng = np.random.default_rng(seed)
+
+    def smooth(a):
+        pad = np.pad(a, 2, mode="edge")
+        return sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
+
+    base = smooth(rng.random((ntheta, ntheta)))
+    direction = smooth(rng.standard_normal((ntheta, ntheta)))
+    direction /= np.max(np.abs(direction))
+    dx = 1e-3
+    reqs, t = [], 0.0
+    for _ in range(R):
+        t += rng.exponential(1.0 / rate)
+        n = int(rng.uniform(*n_range))
+        side = max(2, int(round(math.sqrt(n))))
+        steps = int(rng.uniform(*steps_range))
+        step = math.exp(rng.uniform(math.log(1e-3), math.log(1e-1)))
+        H = side * dx
+        h = 1.3 * dx
+        c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+        p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0,
+                 Lx=2.0 * H, Ly=1.25 * H, kw=5e4, ngx=ntheta, ngy=ntheta)
+        xs = dx + dx * np.arange(side)
+        X, Y = np.meshgrid(xs, xs)
+        X0 = np.vstack([X.ravel(), Y.ravel()]) + rng.uniform(-0.05 * dx, 0.05 * dx,
+                                                               (2, side * side))
+        theta = np.clip(base + step * direction, 0.0, 1.0)
+        reqs.append(dict(t=t, p=p, X0=X0, V0=np.zeros_like(X0), theta=theta, steps=steps,
+                         snapshots=snapshots))
+    return reqs
+
+
+def run_served(args):
+    """Poisson request stream through the continuous-batching server vs the
+    same stream served one request at a time (one worker)."""
+    import torch
+    import sphadjoint_gb300 as S
+    from sphadjoint_gb300.serve import Server
+
+    torch.cuda.set_device(0)
+    S.load()
+    out = {}
+    rates = [float(r) for r in args.rates.split(",")]
+    for mode, workers in (("served", args.workers), ("plain", 1)):
+        res = []
+        for rate in rates:
+            reqs = served_requests(args.requests, rate)
+            with Server(workers=workers, hbm_budget_bytes=int(args.hbm_budget_gb * (1 << 30)),
+                        dtype=args.dtype) as srv:
+                # warm the allocator pool and the code paths
+                w = served_requests(2, 1000.0, seed=99, n_range=(2000, 4000),
+                                    steps_range=(50, 60))
+                for q in w:
+                    srv.submit(S.SPHParams(**q["p"], dtype=args.dtype), q["X0"], q["V0"],
+                               q["theta"], q["steps"], snapshots=q["snapshots"]).wait()
+                srv.reset_stats()
+                srv.tickets.clear()
+                t0 = time.perf_counter()
+                tickets = []
+                for q in reqs:
+                    delay = q["t"] - (time.perf_counter() - t0)
+                    if delay > 0:
+                        time.sleep(delay)
+                    tickets.append(srv.submit(S.SPHParams(**q["p"], dtype=args.dtype), q["X0"],
+                                              q["V0"], q["theta"], q["steps"],
+                                              snapshots=q["snapshots"]))
+                for tk in tickets:
+                    tk.wait()
+                st = srv.stats()
+            ps = sum(q["X0"].shape[1] * q["steps"] for q in reqs)
+            res.append({"rate_per_s": rate, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                        "particle_steps_per_s": st["particle_steps_per_s"],
+                        "completed": st["completed"], "peak_inflight": st["peak_inflight"],
+                        "peak_admitted_gb": st["peak_bytes"] / (1 << 30),
+                        "particle_steps": ps})
+        out[mode] = res
+    cfg = {"workload": "served topology-optimisation line search: Poisson arrivals, N uniform "
+                       "in [2k, 200k], steps uniform in [500, 5000], theta = base 128x128 + "
+                       "log-uniform step along a fixed direction, 32 checkpoints per request",
+           "requests_per_rate": args.requests, "rates": rates, "workers": args.workers,
+           "hbm_budget_gb": args.hbm_budget_gb}
+    best = max(out["served"], key=lambda r: r["particle_steps_per_s"])
+    line = {"metric": "served fwd+adjoint particle-steps/s and p50/p99 latency vs plain",
+            "value": best["particle_steps_per_s"], "unit": "particle-steps/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": args.dtype, "data": "synthetic", "config": cfg,
+            "served": out["served"], "plain": out["plain"]}
+    print(json.dumps(line))
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -490,7 +585,11 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="single", choices=["single", "batched"])
+    ap.add_argument("--workload", default="single", choices=["single", "batched", "served"])
+    ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
+    ap.add_argument("--rates", default="10,100,500", help="served: arrival rates (1/s)")
+    ap.add_argument("--workers", type=int, default=6, help="served: concurrent requests")
+    ap.add_argument("--hbm-budget-gb", type=float, default=96.0, help="served: admission budget")
     ap.add_argument("--instances", type=int, default=64, help="batched: number of instances")
     ap.add_argument("--side", type=int, default=1024, help="lattice side (particles = side^2)")
     ap.add_argument("--nsteps", type=int, default=1000)
@@ -514,6 +613,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_ours(args)
 

@@ -190,6 +190,49 @@ SPH_API int32_t sph_batch_take_flags(sph_state st, uint32_t *flags);
 SPH_API int32_t sph_batch_objective(sph_workspace ws, sph_state st, int32_t kind,
                                     const double *args, double *J);
 
+/* ---- request server (continuous batching) ----
+   No counterpart in the reference, whose optimisation driver calls
+   simulate!/backward! one solve at a time (scripts/03_optimize.jl:228-254).
+   `workers` host threads, each with its own CUDA stream, take forward+adjoint
+   requests FIFO as soon as a worker is free and the request's device memory
+   (states, tape or checkpoints, workspace; sph_request_bytes) fits within
+   hbm_budget_bytes next to the requests already running: requests join while
+   others run and their kernels overlap on the device. Each result equals the
+   same request solved alone. Host inputs of a request (X0, V0, theta) must
+   stay valid, and its outputs (gX, gV, gtheta; any may be NULL) are written,
+   before sph_server_wait returns. Wait for every ticket before destroying. */
+typedef struct sph_server_s *sph_server;
+typedef struct sph_request {
+    sph_params p;
+    int64_t N;
+    const void *X0, *V0;   /* (2, N) T, host */
+    const void *theta;     /* (ngy, ngx) column-major T, host */
+    int64_t nsteps;
+    int32_t snapshots;     /* 0: full tape; c > 0: binomial checkpoints */
+    int32_t objective;     /* SPH_OBJ_KE_RIGHT or SPH_OBJ_TARGET */
+    double obj_args[3];    /* (xc, yc, sigma) for SPH_OBJ_TARGET */
+    double skin;
+    int32_t interval, maxnb;
+    void *gX, *gV, *gtheta; /* host outputs */
+} sph_request;
+SPH_API int32_t sph_server_create(int32_t workers, int64_t hbm_budget_bytes, int32_t dtype,
+                                  sph_server *out);
+SPH_API int32_t sph_server_destroy(sph_server s);
+SPH_API int32_t sph_server_submit(sph_server s, const sph_request *req, int64_t *ticket);
+/* blocks until the request is done; J, latency (submit to done) and flags */
+SPH_API int32_t sph_server_wait(sph_server s, int64_t ticket, double *J, double *latency_ms,
+                                uint32_t *flags);
+SPH_API int32_t sph_server_poll(sph_server s, int64_t ticket, int32_t *done);
+/* latency percentiles of completed requests, particle-steps/s over the span
+   from the first submit to the last completion, completed count, peak
+   admitted bytes and peak number of requests in flight */
+SPH_API int32_t sph_server_stats(sph_server s, double *p50_ms, double *p99_ms,
+                                 double *particle_steps_per_s, int64_t *completed,
+                                 int64_t *peak_bytes, int32_t *peak_inflight);
+SPH_API int32_t sph_server_reset_stats(sph_server s);
+/* admission estimate of one request's device bytes */
+SPH_API int64_t sph_request_bytes(const sph_request *req, int32_t dtype);
+
 /* ---- cell list without allocation ----
    No counterpart in the reference. build!(cl, X, p, backend)
    (src/neighbors.jl:97-114) for callers that cannot let a library allocate

@@ -41,6 +41,14 @@ class ArgumentError(SPHError, ValueError):
     pass
 
 
+class sph_request(C.Structure):
+    _fields_ = [("p", sph_params), ("N", C.c_int64), ("X0", C.c_void_p), ("V0", C.c_void_p),
+                ("theta", C.c_void_p), ("nsteps", C.c_int64), ("snapshots", C.c_int32),
+                ("objective", C.c_int32), ("obj_args", C.c_double * 3), ("skin", C.c_double),
+                ("interval", C.c_int32), ("maxnb", C.c_int32), ("gX", C.c_void_p),
+                ("gV", C.c_void_p), ("gtheta", C.c_void_p)]
+
+
 _P = C.c_void_p
 _PP = C.POINTER(C.c_void_p)
 _I32 = C.c_int32
@@ -94,6 +102,14 @@ _SIGS = {
     "sph_batch_size": (_I32, [_P, _I32P]),
     "sph_batch_take_flags": (_I32, [_P, _U32P]),
     "sph_batch_objective": (_I32, [_P, _P, _I32, _DP, _DP]),
+    "sph_server_create": (_I32, [_I32, _I64, _I32, _PP]),
+    "sph_server_destroy": (_I32, [_P]),
+    "sph_server_submit": (_I32, [_P, C.POINTER(sph_request), _I64P]),
+    "sph_server_wait": (_I32, [_P, _I64, _DP, _DP, _U32P]),
+    "sph_server_poll": (_I32, [_P, _I64, _I32P]),
+    "sph_server_stats": (_I32, [_P, _DP, _DP, _DP, _I64P, _I64P, _I32P]),
+    "sph_server_reset_stats": (_I32, [_P]),
+    "sph_request_bytes": (_I64, [C.POINTER(sph_request), _I32]),
     "sph_launch_count": (_I64, []),
     "sph_profile_enable": (_I32, [_I32, _I32]),
     "sph_profile_read": (_I32, [_I32, _DP, _I64P]),

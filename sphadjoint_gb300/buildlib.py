@@ -26,6 +26,7 @@ SOURCES = {
     "sph_f32.cu": ["--fmad=true"],
     "sph_capi.cu": [],
     "sph_noalloc.cu": ["--fmad=false"],
+    "sph_server.cu": [],
 }
 DEPS = ["sph_common.cuh", "sph_kernels.cuh", "sph_engine.cuh", "sph_iface.hpp"]
 

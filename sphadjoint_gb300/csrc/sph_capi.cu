@@ -20,9 +20,11 @@ namespace sphgb {
 // ---------------------------------------------------------------------------
 namespace {
 thread_local std::string g_err;
-cudaStream_t g_stream = nullptr;
-bool g_stream_external = false;
+thread_local cudaStream_t g_stream = nullptr;
+thread_local bool g_stream_external = false;
 std::atomic<long long> g_launches{0};
+std::mutex g_pool_mu;
+bool g_pool_ready[64] = {};
 
 struct KTimer {
     bool on = false;
@@ -54,6 +56,34 @@ void rt_set_stream(cudaStream_t s)
 {
     g_stream = s;
     g_stream_external = s != nullptr;
+}
+
+// Keep freed blocks in the device's default pool instead of returning them to
+// the driver, so per-request allocations are served from the cache.
+static void pool_init()
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return;
+    std::lock_guard<std::mutex> g(g_pool_mu);
+    if (g_pool_ready[dev]) return;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;
+        (void)cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+    (void)cudaGetLastError();
+    g_pool_ready[dev] = true;
+}
+
+cudaError_t rt_malloc(void **p, size_t bytes, cudaStream_t s)
+{
+    pool_init();
+    return cudaMallocAsync(p, bytes, s);
+}
+
+void rt_free(void *p, cudaStream_t s)
+{
+    if (cudaFreeAsync(p, s) != cudaSuccess) (void)cudaGetLastError();
 }
 
 static cudaEvent_t timer_event(KTimer &t)

@@ -27,20 +27,25 @@
 
 namespace sphgb {
 
+// Device array from the stream-ordered allocator: allocated and freed on the
+// stream of the thread that created it, so freeing one request's buffers
+// does not synchronise the device under other requests' work.
 template <typename T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
+    cudaStream_t s = nullptr;
     DevBuf() {}
     explicit DevBuf(size_t count) { alloc(count); }
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
-    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
     DevBuf &operator=(DevBuf &&o) noexcept
     {
         if (this != &o) {
             release();
             p = o.p;
             n = o.n;
+            s = o.s;
             o.p = nullptr;
             o.n = 0;
         }
@@ -52,19 +57,20 @@ template <typename T> struct DevBuf {
         release();
         n = count;
         if (count) {
-            cudaError_t e = cudaMalloc((void **)&p, sizeof(T) * count);
+            s = rt_stream();
+            cudaError_t e = rt_malloc((void **)&p, sizeof(T) * count, s);
             if (e != cudaSuccess) {
                 p = nullptr;
                 n = 0;
                 (void)cudaGetLastError();
                 throw Error(e == cudaErrorMemoryAllocation ? ERR_NOMEM : ERR_CUDA,
-                            std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+                            std::string("device allocation failed: ") + cudaGetErrorString(e));
             }
         }
     }
     void release()
     {
-        if (p) cudaFree(p);
+        if (p) rt_free(p, s);
         p = nullptr;
         n = 0;
     }

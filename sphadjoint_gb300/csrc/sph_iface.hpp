@@ -66,8 +66,14 @@ enum KernelId : int32_t {
     K_COUNT
 };
 
+// The library stream of the calling host thread (created on first use unless
+// the thread set its own with rt_set_stream).
 cudaStream_t rt_stream();
 void rt_set_stream(cudaStream_t s);
+// Stream-ordered device allocation (the device's default memory pool, kept
+// cached between requests).
+cudaError_t rt_malloc(void **p, size_t bytes, cudaStream_t s);
+void rt_free(void *p, cudaStream_t s);
 void rt_before_launch(int kid);
 void rt_after_launch(int kid);
 void rt_check_launch(const char *name);

@@ -1,0 +1,368 @@
+// Request server for forward + adjoint solves (no counterpart in the
+// reference: its topology-optimisation driver, scripts/03_optimize.jl:228-254,
+// calls simulate!/backward! one solve at a time).
+//
+// Continuous batching: W worker threads, each with its own CUDA stream, take
+// requests from a FIFO queue as soon as a worker is free and the request's
+// device memory (state, tape or checkpoints, workspace) fits in the HBM budget
+// next to the requests already running. Requests therefore join while others
+// are on the GPU, and their kernels run concurrently on the device. Each
+// request runs the same deterministic kernels as a solo call, so its result
+// does not depend on what else is in flight.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/sphadjoint_gb300.h"
+#include "sph_iface.hpp"
+
+namespace sphgb {
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Req {
+    int64_t ticket = 0;
+    sph_request spec{};
+    int64_t bytes = 0;
+    Clock::time_point submitted, started, finished;
+    int status = 0; // 0 queued, 1 running, 2 done, 3 failed
+    double J = 0.0;
+    uint32_t flags = 0;
+    int32_t err = SPH_OK;
+    std::string msg;
+};
+
+// Device bytes a request holds while it runs (the admission estimate): two
+// States (the solve and the reverse scratch) and a recompute State for
+// checkpoint tapes, the adjoint workspace, and the tape itself.
+int64_t request_bytes(const sph_request &r, int dtype)
+{
+    const int64_t s = dtype == SPH_F64 ? 8 : 4;
+    const int64_t N = std::max<int64_t>(r.N, 1);
+    const int64_t state = N * (12 * s + 64);   // positions, velocities, neighbour masks, ...
+    const int64_t work = N * (22 * s + 8);     // gX, gV, abar, gXs, seeds, outputs, ...
+    const double rc = 2.0 * r.p.h * (1.0 + r.skin);
+    const int64_t cells = (int64_t)((r.p.Lx / rc + 3) * (r.p.Ly / rc + 3));
+    const int64_t nodes = (int64_t)r.p.ngx * r.p.ngy;
+    int64_t tape;
+    if (r.snapshots > 0)
+        tape = (int64_t)r.snapshots * (N * (6 * s + 40) + 4 * cells) + state;
+    else
+        tape = std::max<int64_t>(r.nsteps, 1) * N * 4 * s;
+    return 3 * state + work + tape + 8 * cells + 40 * nodes + (16 << 20);
+}
+
+class Server {
+  public:
+    Server(int workers, int64_t budget, int dtype) : budget_(budget), dtype_(dtype)
+    {
+        if (workers < 1) throw Error(ERR_ARG, "need at least one worker");
+        if (budget <= 0) throw Error(ERR_ARG, "HBM budget must be positive");
+        if (dtype != SPH_F64 && dtype != SPH_F32) throw Error(ERR_DTYPE, "bad dtype");
+        cuda_check(cudaGetDevice(&device_), "cudaGetDevice");
+        for (int w = 0; w < workers; ++w) threads_.emplace_back([this] { run(); });
+    }
+
+    ~Server()
+    {
+        {
+            std::lock_guard<std::mutex> g(mu_);
+            stop_ = true;
+        }
+        cv_work_.notify_all();
+        for (auto &t : threads_) t.join();
+    }
+
+    int64_t submit(const sph_request &r)
+    {
+        if (r.N < 1 || r.nsteps < 1) throw Error(ERR_ARG, "request needs N >= 1 and nsteps >= 1");
+        if (!r.X0 || !r.V0 || !r.theta) throw Error(ERR_ARG, "request inputs are NULL");
+        if (r.objective != SPH_OBJ_KE_RIGHT && r.objective != SPH_OBJ_TARGET)
+            throw Error(ERR_ARG, "unknown objective");
+        auto q = std::make_shared<Req>();
+        q->spec = r;
+        q->bytes = request_bytes(r, dtype_);
+        if (q->bytes > budget_)
+            throw Error(ERR_NOMEM, "request needs ~" + std::to_string(q->bytes >> 20) +
+                                       " MiB, more than the whole HBM budget");
+        std::lock_guard<std::mutex> g(mu_);
+        q->ticket = ++next_;
+        q->submitted = Clock::now();
+        if (!anySubmitted_) {
+            first_ = q->submitted;
+            anySubmitted_ = true;
+        }
+        queue_.push_back(q);
+        reqs_[q->ticket] = q;
+        cv_work_.notify_all();
+        return q->ticket;
+    }
+
+    std::shared_ptr<Req> find(int64_t t)
+    {
+        auto it = reqs_.find(t);
+        if (it == reqs_.end()) throw Error(ERR_ARG, "unknown ticket");
+        return it->second;
+    }
+
+    void wait(int64_t t, double *J, double *lat, uint32_t *flags)
+    {
+        std::unique_lock<std::mutex> g(mu_);
+        auto q = find(t);
+        cv_done_.wait(g, [&] { return q->status >= 2; });
+        if (q->status == 3) throw Error(q->err, q->msg);
+        if (J) *J = q->J;
+        if (lat) *lat = std::chrono::duration<double, std::milli>(q->finished - q->submitted).count();
+        if (flags) *flags = q->flags;
+    }
+
+    int poll(int64_t t)
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        return find(t)->status >= 2 ? 1 : 0;
+    }
+
+    void stats(double *p50, double *p99, double *pss, int64_t *done, int64_t *peakBytes,
+               int32_t *peakInflight)
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        std::vector<double> lat = lat_;
+        std::sort(lat.begin(), lat.end());
+        auto pct = [&](double f) {
+            if (lat.empty()) return 0.0;
+            const double k = f * (lat.size() - 1);
+            const size_t a = (size_t)k;
+            const size_t b = std::min(a + 1, lat.size() - 1);
+            return lat[a] + (lat[b] - lat[a]) * (k - a);
+        };
+        if (p50) *p50 = pct(0.50);
+        if (p99) *p99 = pct(0.99);
+        const double span = anyDone_ ? std::chrono::duration<double>(last_ - first_).count() : 0.0;
+        if (pss) *pss = span > 0 ? psteps_ / span : 0.0;
+        if (done) *done = (int64_t)lat.size();
+        if (peakBytes) *peakBytes = peakBytes_;
+        if (peakInflight) *peakInflight = peakInflight_;
+    }
+
+    void reset_stats()
+    {
+        std::lock_guard<std::mutex> g(mu_);
+        lat_.clear();
+        psteps_ = 0;
+        anySubmitted_ = anyDone_ = false;
+        peakBytes_ = 0;
+        peakInflight_ = 0;
+        for (auto it = reqs_.begin(); it != reqs_.end();)
+            it = it->second->status >= 2 ? reqs_.erase(it) : std::next(it);
+    }
+
+  private:
+    void run()
+    {
+        cudaSetDevice(device_);
+        cudaStream_t s = nullptr;
+        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        rt_set_stream(s);
+        for (;;) {
+            std::shared_ptr<Req> q;
+            {
+                std::unique_lock<std::mutex> g(mu_);
+                // FIFO admission: the head of the queue starts when its memory
+                // fits next to the requests already running
+                cv_work_.wait(g, [&] {
+                    return stop_ ||
+                           (!queue_.empty() && inflight_ + queue_.front()->bytes <= budget_);
+                });
+                if (stop_) break;
+                q = queue_.front();
+                queue_.pop_front();
+                inflight_ += q->bytes;
+                ++running_;
+                peakBytes_ = std::max(peakBytes_, inflight_);
+                peakInflight_ = std::max(peakInflight_, running_);
+                q->status = 1;
+                q->started = Clock::now();
+            }
+            const bool ok = solve(*q);
+            {
+                std::lock_guard<std::mutex> g(mu_);
+                inflight_ -= q->bytes;
+                --running_;
+                q->finished = Clock::now();
+                q->status = ok ? 2 : 3;
+                if (ok) {
+                    lat_.push_back(
+                        std::chrono::duration<double, std::milli>(q->finished - q->submitted).count());
+                    psteps_ += (double)q->spec.N * (double)q->spec.nsteps;
+                    last_ = q->finished;
+                    anyDone_ = true;
+                }
+            }
+            cv_work_.notify_all();
+            cv_done_.notify_all();
+        }
+        rt_set_stream(nullptr);
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+
+    // Runs one request on this worker's stream; results go to the caller's
+    // host buffers. Returns false (with q.err / q.msg set) on failure.
+    bool solve(Req &q)
+    {
+        const sph_request &r = q.spec;
+        try {
+            Params p;
+            p.h = r.p.h; p.m = r.p.m; p.rho0 = r.p.rho0; p.c = r.p.c; p.mu = r.p.mu;
+            p.gx = r.p.gx; p.gy = r.p.gy; p.dt = r.p.dt; p.Lx = r.p.Lx; p.Ly = r.p.Ly;
+            p.kw = r.p.kw; p.ngx = r.p.ngx; p.ngy = r.p.ngy;
+            const NLOpts o{r.skin, r.interval, r.maxnb};
+            const std::vector<Params> ps{p};
+            const std::vector<int64_t> ns{r.N};
+            const std::vector<int> gx{p.ngx}, gy{p.ngy};
+            const bool f64 = dtype_ == SPH_F64;
+            std::unique_ptr<StateI> st(f64 ? make_state_f64(ps, ns, r.X0, r.V0, o)
+                                           : make_state_f32(ps, ns, r.X0, r.V0, o));
+            std::unique_ptr<FieldI> th(f64 ? make_field_f64(gx, gy, r.theta)
+                                           : make_field_f32(gx, gy, r.theta));
+            std::unique_ptr<TapeI> tp(f64 ? make_tape_f64(r.N, r.nsteps, r.snapshots)
+                                          : make_tape_f32(r.N, r.nsteps, r.snapshots));
+            std::unique_ptr<WorkI> ws(f64 ? make_work_f64(ps, ns) : make_work_f32(ps, ns));
+            st->simulate(th.get(), nullptr, r.nsteps, tp.get());
+            uint32_t f = st->take_flags();
+            double J = 0.0;
+            ws->objective(st.get(), r.objective, r.objective == SPH_OBJ_TARGET ? r.obj_args : nullptr,
+                          nullptr, &J);
+            uint32_t fb = 0;
+            ws->backward_seeded(tp.get(), th.get(), &p, nullptr, o, &fb);
+            ws->get(r.gX, r.gV, r.gtheta);
+            q.J = J;
+            q.flags = f | fb;
+            return true;
+        } catch (const Error &e) {
+            q.err = e.code;
+            q.msg = e.what();
+        } catch (const std::exception &e) {
+            q.err = ERR_STATE;
+            q.msg = e.what();
+        }
+        (void)cudaStreamSynchronize(rt_stream());
+        return false;
+    }
+
+    const int64_t budget_;
+    const int dtype_;
+    int device_ = 0;
+    std::mutex mu_;
+    std::condition_variable cv_work_, cv_done_;
+    std::deque<std::shared_ptr<Req>> queue_;
+    std::map<int64_t, std::shared_ptr<Req>> reqs_;
+    std::vector<std::thread> threads_;
+    bool stop_ = false;
+    int64_t next_ = 0;
+    int64_t inflight_ = 0, peakBytes_ = 0;
+    int32_t running_ = 0, peakInflight_ = 0;
+    std::vector<double> lat_;
+    double psteps_ = 0;
+    bool anySubmitted_ = false, anyDone_ = false;
+    Clock::time_point first_, last_;
+};
+
+template <typename F> int32_t guard(F &&f)
+{
+    try {
+        f();
+        return SPH_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return SPH_ERR_STATE;
+    }
+}
+
+} // namespace
+} // namespace sphgb
+
+using namespace sphgb;
+#define SV(x) reinterpret_cast<Server *>(x)
+
+extern "C" {
+
+SPH_API int32_t sph_server_create(int32_t workers, int64_t hbm_budget_bytes, int32_t dtype,
+                                  sph_server *out)
+{
+    return guard([&] {
+        if (!out) throw Error(ERR_ARG, "out is NULL");
+        *out = reinterpret_cast<sph_server>(new Server(workers, hbm_budget_bytes, dtype));
+    });
+}
+
+SPH_API int32_t sph_server_destroy(sph_server s)
+{
+    return guard([&] { delete SV(s); });
+}
+
+SPH_API int32_t sph_server_submit(sph_server s, const sph_request *req, int64_t *ticket)
+{
+    return guard([&] {
+        if (!s || !req) throw Error(ERR_ARG, "NULL server or request");
+        const int64_t t = SV(s)->submit(*req);
+        if (ticket) *ticket = t;
+    });
+}
+
+SPH_API int32_t sph_server_wait(sph_server s, int64_t ticket, double *J, double *latency_ms,
+                                uint32_t *flags)
+{
+    return guard([&] {
+        if (!s) throw Error(ERR_ARG, "NULL server");
+        SV(s)->wait(ticket, J, latency_ms, flags);
+    });
+}
+
+SPH_API int32_t sph_server_poll(sph_server s, int64_t ticket, int32_t *done)
+{
+    return guard([&] {
+        if (!s) throw Error(ERR_ARG, "NULL server");
+        const int d = SV(s)->poll(ticket);
+        if (done) *done = d;
+    });
+}
+
+SPH_API int32_t sph_server_stats(sph_server s, double *p50_ms, double *p99_ms,
+                                 double *particle_steps_per_s, int64_t *completed,
+                                 int64_t *peak_bytes, int32_t *peak_inflight)
+{
+    return guard([&] {
+        if (!s) throw Error(ERR_ARG, "NULL server");
+        SV(s)->stats(p50_ms, p99_ms, particle_steps_per_s, completed, peak_bytes, peak_inflight);
+    });
+}
+
+SPH_API int32_t sph_server_reset_stats(sph_server s)
+{
+    return guard([&] {
+        if (!s) throw Error(ERR_ARG, "NULL server");
+        SV(s)->reset_stats();
+    });
+}
+
+SPH_API int64_t sph_request_bytes(const sph_request *req, int32_t dtype)
+{
+    return req ? request_bytes(*req, dtype) : 0;
+}
+
+} // extern "C"
