@@ -128,6 +128,10 @@ def run_batched(args):
     ws = S.BatchWorkspace(bt)
     Jb = (C.c_double * len(inst))()
 
+    if args.autotune:
+        b6 = (C.c_int32 * 6)()
+        LB.check(L.sph_autotune(bt.h, th.h, 5, b6))
+
     def solve_batch():
         LB.check(L.sph_state_assign(bt.h, bt0.h))
         tape.reset()
@@ -338,6 +342,25 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def replicas_value(ms_local, particle_steps_local):
+    """Whole-job throughput of independent replicas (one solve stream per
+    rank, no data-path collective): the slowest rank's time bounds the job,
+    and every rank's work counts. Returns (ms_max, particle-steps/s)."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(ms_local), float(particle_steps_local)], dtype=torch.float64)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        ms = t[:1].to(dev)
+        work = t[1:].to(dev)
+        dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+        dist.all_reduce(work, op=dist.ReduceOp.SUM)
+        t = torch.cat([ms.cpu(), work.cpu()])
+    ms_max, work = float(t[0]), float(t[1])
+    return ms_max, work / (ms_max / 1000.0)
+
+
 def dist_info():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -445,6 +468,13 @@ def run_ours(args):
         LB.check(L.sph_backward_seeded(ws.h, tape.h, th.h, C.byref(pc), None, 0.2, 4, 64,
                                        C.byref(flags)))
 
+    blocks = None
+    if args.autotune:
+        # block sizes measured on this workload's initial state
+        b6 = (C.c_int32 * 6)()
+        LB.check(L.sph_autotune(st.h, th.h, 5, b6))
+        blocks = dict(zip(["nl_build", "density", "accel_integrate", "accel_drag", "pass1",
+                           "pass2"], list(b6)))
     for _ in range(args.warmup):
         solve()
     torch.cuda.synchronize()
@@ -472,13 +502,7 @@ def run_ours(args):
     LB.check(L.sph_profile_read(kid, C.byref(kms), C.byref(kn)))
     LB.check(L.sph_profile_enable(kid, 0))
     rec = tape.recomputed_steps()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-
-    ps = N * args.nsteps * args.steps * world
-    value = ps / (ms / 1000.0)
+    ms, value = replicas_value(ms, N * args.nsteps * args.steps)
     esz = 4 if args.dtype == "f32" else 8
     hbm, peak_kind = peaks()
     if not args.kernel_events:
@@ -573,7 +597,8 @@ def run_ours(args):
                 "data": "synthetic", "config": cfg, "roofline": roof, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "recomputed_forward_steps_per_solve": rec,
-                "objective_J": J.value, "kernels_one_solve": kernels}
+                "objective_J": J.value, "kernels_one_solve": kernels,
+                "block_sizes": blocks}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -608,6 +633,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--breakdown", type=int, default=1)
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="measure per-kernel block sizes on the workload before timing")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -254,6 +254,16 @@ SPH_API int32_t sph_build_cells_noalloc(const void *X_dev, int64_t N, int32_t dt
                                         int32_t nx, int32_t ny, int32_t *counts_dev,
                                         int32_t *starts_dev, int32_t *order_dev, void *stream);
 
+/* Block-size autotuner (no counterpart in the reference, which leaves the
+   workgroup size to KernelAbstractions): times the neighbour-list build,
+   density, accel+integrate and the three adjoint passes at 64/128/256 threads
+   per block on this state's current positions (reps launches each) and uses
+   the fastest from then on for every object of the same precision and kind
+   (single or batched). blocks[6] (may be NULL) receives the choices in that
+   order. Runs on the state's own arrays and a temporary workspace; the state's
+   positions and velocities are not changed. */
+SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_t *blocks);
+
 /* ---- instrumentation ---- */
 /* kernels launched by this library since load */
 SPH_API int64_t sph_launch_count(void);

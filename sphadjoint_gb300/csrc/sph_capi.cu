@@ -468,6 +468,18 @@ SPH_API int32_t sph_backward(sph_workspace ws, sph_tape tp, sph_field theta, con
     });
 }
 
+SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_t *blocks)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(theta, "theta");
+        int b[6] = {0, 0, 0, 0, 0, 0};
+        ST(st)->autotune(FD(theta), reps, b);
+        if (blocks)
+            for (int k = 0; k < 6; ++k) blocks[k] = b[k];
+    });
+}
+
 SPH_API int32_t sph_state_assign(sph_state dst, sph_state src)
 {
     return guarded([&] {

@@ -75,7 +75,8 @@ template <typename T> struct NLView {
     const T2<T> *pos;
     const T2<T> *xref;
     const uint32_t *center;   // cx | cy << 16 | spill << 31 (1-based, instance grid)
-    const uint64_t *masks;    // 3 rows, slot-major: masks[r * N + i]
+    const uint32_t *masks;    // 6 words (row r: words 2r low, 2r+1 high), masks[w * N + i]
+    const uint32_t *tmask;    // this step's words with r^2 < 4h^2 (nullptr: use masks)
     const int32_t *cellStart; // packed table, total cells + 1 exclusive offsets
     const Inst<T> *inst;      // instance table
     const uint16_t *pinst;    // instance of each slot (nullptr: one instance)
@@ -129,9 +130,10 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, const Inst
         // others keep visiting neighbours, so a warp pays for its largest
         // total neighbour count rather than the sum of its per-row maxima.
         const int row0 = I.coff + (jx0 - 1) + (cy - 2) * I.nx; // cell (jx0, cy - 1)
-        const uint64_t m0 = v.masks[i];
-        const uint64_t m1 = v.masks[v.N + i];
-        const uint64_t m2 = v.masks[2 * v.N + i];
+        const uint32_t *mk = v.tmask ? v.tmask : v.masks;
+        const uint64_t m0 = ((uint64_t)mk[v.N + i] << 32) | mk[i];
+        const uint64_t m1 = ((uint64_t)mk[3 * v.N + i] << 32) | mk[2 * v.N + i];
+        const uint64_t m2 = ((uint64_t)mk[5 * v.N + i] << 32) | mk[4 * v.N + i];
         const int b0 = m0 ? v.cellStart[row0] : 0;
         const int b1 = m1 ? v.cellStart[row0 + I.nx] : 0;
         const int b2 = m2 ? v.cellStart[row0 + 2 * I.nx] : 0;

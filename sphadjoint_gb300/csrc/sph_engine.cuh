@@ -81,6 +81,26 @@ template <typename T> struct DevBuf {
 
 inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
+// Threads per block of each tuned kernel, per precision and per single/batched
+// variant; 256 until autotune() has measured the candidates on a real state.
+template <typename T> int &tuned_block(int kid, bool multi)
+{
+    static int tab[K_COUNT][2] = {};
+    int &b = tab[kid][multi ? 1 : 0];
+    if (b == 0) b = kBlock;
+    return b;
+}
+
+#define SPH_LAUNCH_TUNED(kid, multi, kern, n, ...)                                            \
+    do {                                                                                      \
+        if ((n) > 0) {                                                                        \
+            const int bs_ = ::sphgb::tuned_block<T>(kid, multi);                              \
+            ::sphgb::rt_before_launch(kid);                                                   \
+            kern<<<(unsigned)(((n) + bs_ - 1) / bs_), bs_, 0, ::sphgb::rt_stream()>>>(__VA_ARGS__); \
+            ::sphgb::rt_after_launch(kid);                                                    \
+        }                                                                                     \
+    } while (0)
+
 #define SPH_LAUNCH(kid, kern, n, ...)                                                         \
     do {                                                                                      \
         if ((n) > 0) {                                                                        \
@@ -182,7 +202,7 @@ template <typename T> struct Snap {
     DevBuf<T2<T>> pos, vel, xref;
     DevBuf<int32_t> perm, invperm, cellStart, nbcount;
     DevBuf<uint32_t> center;
-    DevBuf<uint64_t> masks;
+    DevBuf<uint32_t> masks;
     int64_t age = INT64_MAX;
     bool valid = false;
 };
@@ -208,7 +228,8 @@ template <typename T> class Sys final : public StateI {
     DevBuf<int32_t> perm, invperm, cellStart, nbcount, cellTmp, counts, cursor, bucketSrc,
         bucketId, scanTmp;
     DevBuf<uint32_t> center, flags;
-    DevBuf<uint64_t> masks;
+    DevBuf<uint32_t> masks;  // 6 words per particle, word-major
+    DevBuf<uint32_t> tmask;  // this step's in-support words (written by the density pass)
     DevBuf<T> rho;
     DevBuf<T2<T>> prho;
     DevBuf<T2<T>> accOut;
@@ -322,7 +343,8 @@ template <typename T> class Sys final : public StateI {
         scanTmp.alloc((size_t)((ncell + kScanTile - 1) / kScanTile + 1));
         center.alloc(n1);
         flags.alloc((size_t)B);
-        masks.alloc(3 * n1);
+        masks.alloc(6 * n1);
+        tmask.alloc(6 * n1);
         rho.alloc(n1);
         prho.alloc(n1);
         stage2.alloc(n1);
@@ -386,6 +408,7 @@ template <typename T> class Sys final : public StateI {
         v.xref = xref.p;
         v.center = center.p;
         v.masks = masks.p;
+        v.tmask = nullptr;
         v.cellStart = cellStart.p;
         v.inst = dinst.p;
         v.pinst = pinst.p;
@@ -487,8 +510,8 @@ template <typename T> class Sys final : public StateI {
                        invperm.p, ex0, ex0N, ex1, ex1N);
             cur = nxt;
             auto kn = B > 1 ? &k_nl_build<T, true> : &k_nl_build<T, false>;
-            SPH_LAUNCH(K_NLBUILD, kn, N_, N_, hinst[0], dinst.p, pinst.p, pos[cur].p, cellStart.p,
-                       center.p, masks.p, nbcount.p, flags.p);
+            SPH_LAUNCH_TUNED(K_NLBUILD, B > 1, kn, N_, N_, hinst[0], dinst.p, pinst.p, pos[cur].p,
+                             cellStart.p, center.p, masks.p, nbcount.p, flags.p);
         }
         age = 0;
         cellsOnlyLatest = false;
@@ -545,14 +568,15 @@ template <typename T> class Sys final : public StateI {
         maybe_rebuild();
         if (N_ == 0) return;
         if (tx) SPH_LAUNCH(K_TAPE, k_tape_store<T>, N_, N_, perm.p, pos[cur].p, vel[cur].p, tx, tv);
-        const NLView<T> v = view();
+        NLView<T> v = view();
         auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
-        SPH_LAUNCH(K_DENSITY, kd, N_, v, rho.p, prho.p);
+        SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rho.p, prho.p, tmask.p);
+        v.tmask = tmask.p;
         const int nxt = 1 - cur;
         auto ki = B > 1 ? &k_accel_integrate<T, true> : &k_accel_integrate<T, false>;
-        SPH_LAUNCH(K_ACCEL_INTEGRATE, ki, N_, v, vel[cur].p, prho.p, theta,
-                   pos[nxt].p, vel[nxt].p, keepAccel ? accOut.p : (T2<T> *)nullptr,
-                   keepAccel ? alphaOut.p : (T *)nullptr, flags.p);
+        SPH_LAUNCH_TUNED(K_ACCEL_INTEGRATE, B > 1, ki, N_, v, vel[cur].p, prho.p, theta,
+                         pos[nxt].p, vel[nxt].p, keepAccel ? accOut.p : (T2<T> *)nullptr,
+                         keepAccel ? alphaOut.p : (T *)nullptr, flags.p);
         cur = nxt;
     }
 
@@ -578,6 +602,7 @@ template <typename T> class Sys final : public StateI {
     }
 
     void simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tape) override;
+    void autotune(FieldI *theta, int reps, int *chosen) override;
 
     void celllist(int32_t *countsOut, int32_t *startsOut, int32_t *orderOut) override
     {
@@ -635,7 +660,7 @@ template <typename T> class Sys final : public StateI {
         s.pos.alloc(n1); s.vel.alloc(n1); s.xref.alloc(n1);
         s.perm.alloc(n1); s.invperm.alloc(n1); s.nbcount.alloc(n1);
         s.cellStart.alloc((size_t)ncell + 1);
-        s.center.alloc(n1); s.masks.alloc(3 * n1);
+        s.center.alloc(n1); s.masks.alloc(6 * n1);
     }
     void save(Snap<T> &s)
     {
@@ -967,20 +992,21 @@ template <typename T> class Work final : public WorkI {
         const int g2 = 1 - gcur;
         S.maybe_rebuild(gX[gcur].p, gX[g2].p, gV[gcur].p, gV[g2].p, &did);
         if (did) gcur = g2;
-        const NLView<T> v = S.view();
+        NLView<T> v = S.view();
         const T2<T> *vel = S.vel[S.cur].p;
         const bool multi = S.B > 1;
         auto kd = multi ? &k_density_eos<T, true> : &k_density_eos<T, false>;
         auto ka = multi ? &k_accel_drag_adj<T, true> : &k_accel_drag_adj<T, false>;
         auto k1 = multi ? &k_pass1_design<T, true> : &k_pass1_design<T, false>;
         auto k2 = multi ? &k_pass2_axpy<T, true> : &k_pass2_axpy<T, false>;
-        SPH_LAUNCH(K_DENSITY, kd, N_, v, (T *)nullptr, S.prho.p);
-        SPH_LAUNCH(K_ACCEL_DRAG, ka, N_, v, vel, S.prho.p, theta, gX[gcur].p, gV[gcur].p, abar.p,
-                   galpha.p, emax.p, parity);
-        SPH_LAUNCH(K_PASS1, k1, N_, v, vel, S.prho.p, theta, abar.p, galpha.p, gXs.p, grho.p,
-                   gV[gcur].p);
-        SPH_LAUNCH(K_PASS2, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p, parity,
-                   thetaAcc.p);
+        SPH_LAUNCH_TUNED(K_DENSITY, multi, kd, N_, v, (T *)nullptr, S.prho.p, S.tmask.p);
+        v.tmask = S.tmask.p;
+        SPH_LAUNCH_TUNED(K_ACCEL_DRAG, multi, ka, N_, v, vel, S.prho.p, theta, gX[gcur].p,
+                         gV[gcur].p, abar.p, galpha.p, emax.p, parity);
+        SPH_LAUNCH_TUNED(K_PASS1, multi, k1, N_, v, vel, S.prho.p, theta, abar.p, galpha.p, gXs.p,
+                         grho.p, gV[gcur].p);
+        SPH_LAUNCH_TUNED(K_PASS2, multi, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p,
+                         parity, thetaAcc.p);
         SPH_LAUNCH(K_THETA_NODE, k_theta_node<T>, nnode, nnode, S.B, S.dinst.p, thetaAcc.p, emax.p,
                    parity, gtheta.p);
     }
@@ -1058,6 +1084,113 @@ template <typename T> class Work final : public WorkI {
         }
     }
 };
+
+// Block-size autotuner: times each hot kernel of this state's kind (single or
+// batched) at 64, 128 and 256 threads per block on the state's current
+// positions and keeps the fastest. Forward kernels run on the state itself
+// (they only write derived arrays); the adjoint kernels run on a temporary
+// workspace with placeholder gradients, whose values do not change the work.
+template <typename T> class Tuner {
+  public:
+    static void run(Sys<T> &S, Field<T> &th, int reps, int *chosen)
+    {
+        if (S.N_ == 0) return;
+        if (S.age == INT64_MAX) S.rebuild();
+        const bool multi = S.B > 1;
+        const int cand[3] = {64, 128, 256};
+        cudaEvent_t e0, e1;
+        SPH_CK(cudaEventCreate(&e0));
+        SPH_CK(cudaEventCreate(&e1));
+        auto timeit = [&](const std::function<void(int)> &launch) {
+            float best = 1e30f;
+            int bestB = kBlock;
+            for (int c : cand) {
+                launch(c); // warm
+                SPH_CK(cudaEventRecord(e0, rt_stream()));
+                for (int r = 0; r < reps; ++r) launch(c);
+                SPH_CK(cudaEventRecord(e1, rt_stream()));
+                SPH_CK(cudaEventSynchronize(e1));
+                float ms = 0;
+                SPH_CK(cudaEventElapsedTime(&ms, e0, e1));
+                if (ms < best) {
+                    best = ms;
+                    bestB = c;
+                }
+            }
+            return bestB;
+        };
+        const int64_t N = S.N_;
+        auto grid = [N](int b) { return (unsigned)((N + b - 1) / b); };
+        cudaStream_t st = rt_stream();
+        NLView<T> v = S.view();
+        const int nxt = 1 - S.cur;
+        auto kn = multi ? &k_nl_build<T, true> : &k_nl_build<T, false>;
+        auto kd = multi ? &k_density_eos<T, true> : &k_density_eos<T, false>;
+        auto ki = multi ? &k_accel_integrate<T, true> : &k_accel_integrate<T, false>;
+        auto ka = multi ? &k_accel_drag_adj<T, true> : &k_accel_drag_adj<T, false>;
+        auto k1 = multi ? &k_pass1_design<T, true> : &k_pass1_design<T, false>;
+        auto k2 = multi ? &k_pass2_axpy<T, true> : &k_pass2_axpy<T, false>;
+        int b;
+        b = timeit([&](int c) {
+            kn<<<grid(c), c, 0, st>>>(N, S.hinst[0], S.dinst.p, S.pinst.p, S.pos[S.cur].p,
+                                      S.cellStart.p, S.center.p, S.masks.p, S.nbcount.p,
+                                      S.flags.p);
+        });
+        tuned_block<T>(K_NLBUILD, multi) = b;
+        b = timeit([&](int c) {
+            kd<<<grid(c), c, 0, st>>>(v, S.rho.p, S.prho.p, S.tmask.p);
+        });
+        tuned_block<T>(K_DENSITY, multi) = b;
+        v.tmask = S.tmask.p;
+        b = timeit([&](int c) {
+            ki<<<grid(c), c, 0, st>>>(v, S.vel[S.cur].p, S.prho.p, th.th.p, S.pos[nxt].p,
+                                      S.vel[nxt].p, nullptr, nullptr, S.flags.p);
+        });
+        tuned_block<T>(K_ACCEL_INTEGRATE, multi) = b;
+        // adjoint passes on placeholder gradients
+        std::vector<int64_t> ns;
+        for (const auto &I : S.hinst) ns.push_back(I.n);
+        Work<T> w(S.prms, ns);
+        for (int k = 0; k < 2; ++k) {
+            SPH_CK(cudaMemsetAsync(w.gX[k].p, 0x3c, w.gX[k].bytes(), st));
+            SPH_CK(cudaMemsetAsync(w.gV[k].p, 0x3c, w.gV[k].bytes(), st));
+        }
+        const std::vector<int> init(2 * (size_t)S.B, INT_MIN);
+        SPH_CK(cudaMemcpyAsync(w.emax.p, init.data(), sizeof(int) * init.size(), cudaMemcpyHostToDevice, st));
+        const T2<T> *vel = S.vel[S.cur].p;
+        ka<<<grid(kBlock), kBlock, 0, st>>>(v, vel, S.prho.p, th.th.p, w.gX[0].p, w.gV[0].p,
+                                            w.abar.p, w.galpha.p, w.emax.p, 0);
+        b = timeit([&](int c) {
+            ka<<<grid(c), c, 0, st>>>(v, vel, S.prho.p, th.th.p, w.gX[0].p, w.gV[1].p, w.abar.p,
+                                      w.galpha.p, w.emax.p, 1);
+        });
+        tuned_block<T>(K_ACCEL_DRAG, multi) = b;
+        b = timeit([&](int c) {
+            k1<<<grid(c), c, 0, st>>>(v, vel, S.prho.p, th.th.p, w.abar.p, w.galpha.p, w.gXs.p,
+                                      w.grho.p, w.gV[1].p);
+        });
+        tuned_block<T>(K_PASS1, multi) = b;
+        b = timeit([&](int c) {
+            w.thetaAcc.zero();
+            k2<<<grid(c), c, 0, st>>>(v, w.grho.p, w.gXs.p, w.gX[1].p, w.galpha.p, w.emax.p, 0,
+                                      w.thetaAcc.p);
+        });
+        tuned_block<T>(K_PASS2, multi) = b;
+        SPH_CK(cudaStreamSynchronize(st));
+        SPH_CK(cudaEventDestroy(e0));
+        SPH_CK(cudaEventDestroy(e1));
+        rt_check_launch("autotune");
+        const int ids[6] = {K_NLBUILD, K_DENSITY, K_ACCEL_INTEGRATE, K_ACCEL_DRAG, K_PASS1, K_PASS2};
+        if (chosen)
+            for (int k = 0; k < 6; ++k) chosen[k] = tuned_block<T>(ids[k], multi);
+    }
+};
+
+template <typename T> void Sys<T>::autotune(FieldI *theta, int reps, int *chosen)
+{
+    Field<T> *th = field_of(theta);
+    Tuner<T>::run(*this, *th, std::max(1, reps), chosen);
+}
 
 template <typename T>
 void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const void *seedX,

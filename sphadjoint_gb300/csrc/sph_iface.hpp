@@ -122,6 +122,7 @@ class StateI {
     virtual void assign(StateI *src) = 0;
     virtual int batch() const = 0;
     virtual void take_flags_batch(uint32_t *per_instance) = 0;
+    virtual void autotune(FieldI *theta, int reps, int *chosen) = 0;
 };
 
 enum ObjectiveKind : int32_t {

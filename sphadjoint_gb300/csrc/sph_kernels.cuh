@@ -221,7 +221,7 @@ template <typename T, bool MULTI>
 __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restrict__ inst,
                            const uint16_t *__restrict__ pinst, const T2<T> *__restrict__ pos,
                            const int32_t *__restrict__ cellStart, uint32_t *__restrict__ center,
-                           uint64_t *__restrict__ masks, int32_t *__restrict__ nbcount,
+                           uint32_t *__restrict__ masks, int32_t *__restrict__ nbcount,
                            uint32_t *__restrict__ flags)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -262,7 +262,8 @@ __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restri
                 }
             }
         }
-        masks[(int64_t)r * N + i] = ((uint64_t)hi << 32) | lo;
+        masks[(int64_t)(2 * r) * N + i] = lo;
+        masks[(int64_t)(2 * r + 1) * N + i] = hi;
     }
     center[i] = (uint32_t)cx | ((uint32_t)cy << 16) | (spill << 31);
     nbcount[i] = m;
@@ -274,9 +275,14 @@ __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restri
 // integrate_kernel! (fused; positions and velocities double-buffered because
 // neighbours read the pre-step state).
 // ---------------------------------------------------------------------------
+// density_kernel! + eos_kernel!. It also records, for the rest of this step,
+// which neighbour-list entries are inside the support (r^2 < 4h^2): the later
+// passes of the step walk only those (same set, same order), skipping the
+// candidates that the reference's own r^2 test would reject.
 template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
-    k_density_eos(const __grid_constant__ NLView<T> v, T *__restrict__ rho, T2<T> *__restrict__ prho)
+    k_density_eos(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
+                  T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
@@ -284,18 +290,63 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
     const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, A = I.p.A;
     const T2<T> xi = v.pos[i];
     T acc = (T)0;
-    for_each_neighbor<T>(v, I, i, [&](int j) {
-        const T2<T> xj = v.pos[j];
-        const T dx = xi.x - xj.x;
-        const T dy = xi.y - xj.y;
-        const T r2 = dx * dx + dy * dy;
-        if (r2 < r2max) {
-            const T q = pair_sqrt(r2) * invh;
-            const T u = (T)1 - (T)0.5 * q;
-            const T u2 = u * u;
-            acc += m * (A * u2 * u2 * ((T)2 * q + (T)1));
+    const uint32_t cc = v.center[i];
+    if (!(cc >> 31)) {
+        // the walk of for_each_neighbor, keeping the passing bits
+        const int cx = (int)(cc & 0xffffu);
+        const int cy = (int)((cc >> 16) & 0x7fffu);
+        const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
+        const int row0 = I.coff + (jx0 - 1) + (cy - 2) * I.nx;
+        const uint64_t m0 = ((uint64_t)v.masks[v.N + i] << 32) | v.masks[i];
+        const uint64_t m1 = ((uint64_t)v.masks[3 * v.N + i] << 32) | v.masks[2 * v.N + i];
+        const uint64_t m2 = ((uint64_t)v.masks[5 * v.N + i] << 32) | v.masks[4 * v.N + i];
+        const int b0 = m0 ? v.cellStart[row0] : 0;
+        const int b1 = m1 ? v.cellStart[row0 + I.nx] : 0;
+        const int b2 = m2 ? v.cellStart[row0 + 2 * I.nx] : 0;
+        uint32_t mw = (uint32_t)m0, tw = 0u;
+        int base = b0;
+        int w = 0;
+        for (;;) {
+            if (mw == 0u) {
+                if (tmaskOut) tmaskOut[(int64_t)w * v.N + i] = tw; // word w is finished
+                tw = 0u;
+                if (++w == 6) break;
+                const uint64_t mr = w < 2 ? m0 : (w < 4 ? m1 : m2);
+                const int br = w < 2 ? b0 : (w < 4 ? b1 : b2);
+                mw = (w & 1) ? (uint32_t)(mr >> 32) : (uint32_t)mr;
+                base = br + ((w & 1) << 5);
+                continue;
+            }
+            const int k = __ffs((int)mw) - 1;
+            mw &= mw - 1u;
+            const T2<T> xj = v.pos[base + k];
+            const T dx = xi.x - xj.x;
+            const T dy = xi.y - xj.y;
+            const T r2 = dx * dx + dy * dy;
+            if (r2 < r2max) {
+                tw |= 1u << k;
+                const T q = pair_sqrt(r2) * invh;
+                const T u = (T)1 - (T)0.5 * q;
+                const T u2 = u * u;
+                acc += m * (A * u2 * u2 * ((T)2 * q + (T)1));
+            }
         }
-    });
+    } else {
+        for_each_neighbor<T>(v, I, i, [&](int j) {
+            const T2<T> xj = v.pos[j];
+            const T dx = xi.x - xj.x;
+            const T dy = xi.y - xj.y;
+            const T r2 = dx * dx + dy * dy;
+            if (r2 < r2max) {
+                const T q = pair_sqrt(r2) * invh;
+                const T u = (T)1 - (T)0.5 * q;
+                const T u2 = u * u;
+                acc += m * (A * u2 * u2 * ((T)2 * q + (T)1));
+            }
+        });
+        if (tmaskOut)
+            for (int w = 0; w < 6; ++w) tmaskOut[(int64_t)w * v.N + i] = 0u;
+    }
     const T ri = acc + m * A;
     if (rho) rho[i] = ri;
     const T inv = (T)1 / ri;

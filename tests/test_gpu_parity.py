@@ -176,3 +176,19 @@ def test_particles_outside_tank_and_single_particle():
     g = run_gpu(one, 5, seeds=linear_seeds(one))
     r = run_oracle(one, 5, seeds=linear_seeds(one))
     assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["gV"], r["gV"])
+
+
+def test_autotuned_block_sizes_do_not_change_results():
+    case = K.adjoint_case(seed=7)
+    seeds = linear_seeds(case)
+    ref = run_gpu(case, 10, seeds=seeds)
+    p = S.SPHParams(**case["p"])
+    st = S.State(case["X0"], case["V0"], p, interval=1)
+    import ctypes as C
+    b6 = (C.c_int32 * 6)()
+    lib = S.load()
+    assert lib.sph_autotune(st.h, S.DesignField(case["theta"]).h, 2, b6) == 0
+    assert all(b in (64, 128, 256) for b in b6)
+    again = run_gpu(case, 10, seeds=seeds)
+    for k in ("X", "V", "gX", "gV", "gtheta"):
+        assert np.array_equal(ref[k], again[k]), k
