@@ -34,11 +34,12 @@ template <typename T> struct DevBuf {
     T *p = nullptr;
     size_t n = 0;
     cudaStream_t s = nullptr;
+    bool own = true; // false: a view into a block owned elsewhere
     DevBuf() {}
     explicit DevBuf(size_t count) { alloc(count); }
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
-    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+    DevBuf(DevBuf &&o) noexcept : p(o.p), n(o.n), s(o.s), own(o.own) { o.p = nullptr; o.n = 0; }
     DevBuf &operator=(DevBuf &&o) noexcept
     {
         if (this != &o) {
@@ -46,15 +47,24 @@ template <typename T> struct DevBuf {
             p = o.p;
             n = o.n;
             s = o.s;
+            own = o.own;
             o.p = nullptr;
             o.n = 0;
         }
         return *this;
     }
     ~DevBuf() { release(); }
+    void view(T *ptr, size_t count)
+    {
+        release();
+        p = ptr;
+        n = count;
+        own = false;
+    }
     void alloc(size_t count)
     {
         release();
+        own = true;
         n = count;
         if (count) {
             s = rt_stream();
@@ -70,7 +80,7 @@ template <typename T> struct DevBuf {
     }
     void release()
     {
-        if (p) rt_free(p, s);
+        if (p && own) rt_free(p, s);
         p = nullptr;
         n = 0;
     }
@@ -198,12 +208,12 @@ template <typename T> class Field final : public FieldI {
 // A copy of everything that determines the future of a Sys: the state in
 // cell order, its permutation, and the neighbour structure of the last
 // rebuild (so recomputation from a snapshot repeats the forward bit for bit).
+// The arrays are one contiguous block (Sys::core), so a snapshot is a single
+// device-to-device copy.
 template <typename T> struct Snap {
-    DevBuf<T2<T>> pos, vel, xref;
-    DevBuf<int32_t> perm, invperm, cellStart, nbcount;
-    DevBuf<uint32_t> center;
-    DevBuf<uint32_t> masks;
+    DevBuf<uint8_t> blob;
     int64_t age = INT64_MAX;
+    int cur = 0;
     bool valid = false;
 };
 
@@ -222,6 +232,7 @@ template <typename T> class Sys final : public StateI {
     double cs_d, rc_d, dmax_d;  // instance 0
     NLOpts opts;
     int64_t age = INT64_MAX;
+    DevBuf<uint8_t> core; // one block holding every array a snapshot must keep
     DevBuf<T2<T>> pos[2], vel[2];
     int cur = 0;
     DevBuf<T2<T>> xref;
@@ -326,14 +337,35 @@ template <typename T> class Sys final : public StateI {
             SPH_CK(cudaMemcpyAsync(pinst.p, pi.data(), sizeof(uint16_t) * n1, cudaMemcpyHostToDevice, rt_stream()));
             SPH_CK(cudaStreamSynchronize(rt_stream()));
         }
-        for (int k = 0; k < 2; ++k) {
-            pos[k].alloc(n1);
-            vel[k].alloc(n1);
+        {
+            // the state that determines the future, in one block: positions and
+            // velocities (both buffers), rebuild positions, permutation, cell
+            // table, cell centres and neighbour masks
+            size_t off = 0;
+            auto carve = [&](size_t bytes) {
+                const size_t o = off;
+                off += (bytes + 255) & ~(size_t)255;
+                return o;
+            };
+            const size_t oPos0 = carve(sizeof(T2<T>) * n1), oPos1 = carve(sizeof(T2<T>) * n1);
+            const size_t oVel0 = carve(sizeof(T2<T>) * n1), oVel1 = carve(sizeof(T2<T>) * n1);
+            const size_t oXref = carve(sizeof(T2<T>) * n1);
+            const size_t oPerm = carve(4 * n1), oInv = carve(4 * n1), oCtr = carve(4 * n1);
+            const size_t oMask = carve(4 * 6 * n1);
+            const size_t oCell = carve(4 * ((size_t)ncell + 1));
+            core.alloc(off);
+            uint8_t *c = core.p;
+            pos[0].view((T2<T> *)(c + oPos0), n1);
+            pos[1].view((T2<T> *)(c + oPos1), n1);
+            vel[0].view((T2<T> *)(c + oVel0), n1);
+            vel[1].view((T2<T> *)(c + oVel1), n1);
+            xref.view((T2<T> *)(c + oXref), n1);
+            perm.view((int32_t *)(c + oPerm), n1);
+            invperm.view((int32_t *)(c + oInv), n1);
+            center.view((uint32_t *)(c + oCtr), n1);
+            masks.view((uint32_t *)(c + oMask), 6 * n1);
+            cellStart.view((int32_t *)(c + oCell), (size_t)ncell + 1);
         }
-        xref.alloc(n1);
-        perm.alloc(n1);
-        invperm.alloc(n1);
-        cellStart.alloc((size_t)ncell + 1);
         nbcount.alloc(n1);
         cellTmp.alloc(n1);
         counts.alloc((size_t)ncell);
@@ -341,9 +373,7 @@ template <typename T> class Sys final : public StateI {
         bucketSrc.alloc(n1);
         bucketId.alloc(n1);
         scanTmp.alloc((size_t)((ncell + kScanTile - 1) / kScanTile + 1));
-        center.alloc(n1);
         flags.alloc((size_t)B);
-        masks.alloc(6 * n1);
         tmask.alloc(6 * n1);
         rho.alloc(n1);
         prho.alloc(n1);
@@ -653,31 +683,21 @@ template <typename T> class Sys final : public StateI {
     void sync() override { SPH_CK(cudaStreamSynchronize(rt_stream())); }
 
     // ---- snapshots ----
-    void snap_alloc(Snap<T> &s) const
-    {
-        const size_t n1 = (size_t)std::max<int64_t>(N_, 1);
-        if (s.pos.p) return;
-        s.pos.alloc(n1); s.vel.alloc(n1); s.xref.alloc(n1);
-        s.perm.alloc(n1); s.invperm.alloc(n1); s.nbcount.alloc(n1);
-        s.cellStart.alloc((size_t)ncell + 1);
-        s.center.alloc(n1); s.masks.alloc(6 * n1);
-    }
     void save(Snap<T> &s)
     {
-        snap_alloc(s);
-        s.pos.copy_from(pos[cur]); s.vel.copy_from(vel[cur]); s.xref.copy_from(xref);
-        s.perm.copy_from(perm); s.invperm.copy_from(invperm); s.nbcount.copy_from(nbcount);
-        s.cellStart.copy_from(cellStart); s.center.copy_from(center); s.masks.copy_from(masks);
+        if (!s.blob.p) s.blob.alloc(core.n);
+        s.blob.copy_from(core);
         s.age = age;
+        s.cur = cur;
         s.valid = true;
     }
     void restore(const Snap<T> &s)
     {
         if (!s.valid) throw Error(ERR_STATE, "restoring an empty snapshot");
-        pos[cur].copy_from(s.pos); vel[cur].copy_from(s.vel); xref.copy_from(s.xref);
-        perm.copy_from(s.perm); invperm.copy_from(s.invperm); nbcount.copy_from(s.nbcount);
-        cellStart.copy_from(s.cellStart); center.copy_from(s.center); masks.copy_from(s.masks);
+        if (s.blob.n != core.n) throw Error(ERR_STATE, "snapshot of another configuration");
+        core.copy_from(s.blob);
         age = s.age;
+        cur = s.cur;
         cellsOnlyLatest = false;
     }
     void assign(StateI *src) override
@@ -686,12 +706,13 @@ template <typename T> class Sys final : public StateI {
         if (!o) throw Error(ERR_DTYPE, "source state has a different precision");
         if (!same_config(*o)) throw Error(ERR_ARG, "source state has another configuration");
         if (o == this) return;
-        pos[cur].copy_from(o->pos[o->cur]); vel[cur].copy_from(o->vel[o->cur]);
-        xref.copy_from(o->xref); perm.copy_from(o->perm); invperm.copy_from(o->invperm);
-        nbcount.copy_from(o->nbcount); cellStart.copy_from(o->cellStart);
-        center.copy_from(o->center); masks.copy_from(o->masks); flags.copy_from(o->flags);
-        rho.copy_from(o->rho); prho.copy_from(o->prho);
+        core.copy_from(o->core);
+        nbcount.copy_from(o->nbcount);
+        flags.copy_from(o->flags);
+        rho.copy_from(o->rho);
+        prho.copy_from(o->prho);
         age = o->age;
+        cur = o->cur;
         if (std::memcmp(hinst.data(), o->hinst.data(), sizeof(Inst<T>) * B) != 0) {
             prm = o->prm;
             prms = o->prms;
@@ -983,11 +1004,35 @@ template <typename T> class Work final : public WorkI {
 
     // One reverse step at the pre-state held in (sx, sv); srcInv maps particle
     // ids into the source's slots when the source is a recomputed state.
+    // The design-node write-back of a reverse step is deferred into the next
+    // step's gather launch (pendingTheta holds its parity) or flush_theta().
+    int pendingTheta = -1;
+
+    void flush_theta(Sys<T> &S)
+    {
+        if (pendingTheta < 0) return;
+        SPH_LAUNCH(K_THETA_NODE, k_theta_node<T>, nnode, nnode, S.B, S.dinst.p, thetaAcc.p, emax.p,
+                   pendingTheta, gtheta.p);
+        pendingTheta = -1;
+    }
+
     void reverse_step(Sys<T> &S, const T *theta, const T2<T> *sx, const T2<T> *sv,
                       const int32_t *srcInv, int parity)
     {
-        SPH_LAUNCH(K_GATHER, k_gather_state<T>, N_, N_, S.perm.p, srcInv, sx, sv, S.pos[S.cur].p,
-                   S.vel[S.cur].p);
+        if (pendingTheta >= 0 && N_ > 0) {
+            const unsigned gN = grid_for(N_);
+            const unsigned gT = grid_for(nnode);
+            rt_before_launch(K_GATHER);
+            k_gather_theta<T><<<gN + gT, kBlock, 0, rt_stream()>>>(
+                N_, gN, S.perm.p, srcInv, sx, sv, S.pos[S.cur].p, S.vel[S.cur].p, nnode, S.B,
+                S.dinst.p, thetaAcc.p, emax.p, pendingTheta, gtheta.p);
+            rt_after_launch(K_GATHER);
+            pendingTheta = -1;
+        } else {
+            flush_theta(S);
+            SPH_LAUNCH(K_GATHER, k_gather_state<T>, N_, N_, S.perm.p, srcInv, sx, sv,
+                       S.pos[S.cur].p, S.vel[S.cur].p);
+        }
         bool did = false;
         const int g2 = 1 - gcur;
         S.maybe_rebuild(gX[gcur].p, gX[g2].p, gV[gcur].p, gV[g2].p, &did);
@@ -1007,8 +1052,7 @@ template <typename T> class Work final : public WorkI {
                          grho.p, gV[gcur].p);
         SPH_LAUNCH_TUNED(K_PASS2, multi, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p,
                          parity, thetaAcc.p);
-        SPH_LAUNCH(K_THETA_NODE, k_theta_node<T>, nnode, nnode, S.B, S.dinst.p, thetaAcc.p, emax.p,
-                   parity, gtheta.p);
+        pendingTheta = parity;
     }
 
     void backward(TapeI *tape, FieldI *theta, const Params *p, const void *seedX,
@@ -1267,6 +1311,7 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     }
 
     const int64_t L = tp->n_;
+    pendingTheta = -1;
     int64_t rstep = 0; // reverse steps done (parity of the exponent slot)
     tp->fwdSteps = 0;
     if (tp->nsnap_ == 0) {
@@ -1290,9 +1335,19 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
         std::vector<int> freeSlots;
         for (int k = C - 1; k >= 0; --k)
             if (tp->slotPos[k] < 0 || tp->slotPos[k] >= L) freeSlots.push_back(k);
+        int64_t rpos = -1; // step the recompute state holds (-1: unknown)
         auto advance = [&](int64_t m) {
             for (int64_t s = 0; s < m; ++s) R.step_impl(th->th.p, nullptr, nullptr);
             tp->fwdSteps += m;
+            rpos += m;
+        };
+        // the recompute state repeats the forward bit for bit, so it already
+        // equals a snapshot of the step it holds
+        auto restore_at = [&](int slot, int64_t a) {
+            if (rpos != a) {
+                R.restore(tp->slot(slot));
+                rpos = a;
+            }
         };
         auto rev_at_R = [&](int64_t n) {
             (void)n;
@@ -1305,20 +1360,20 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
         std::function<void(int64_t, int64_t, int, int64_t)> seg =
             [&](int64_t a, int64_t b, int slot, int64_t c) {
                 if (b - a == 1) {
-                    R.restore(tp->slot(slot));
+                    restore_at(slot, a);
                     rev_at_R(a);
                     return;
                 }
                 if (c <= 1 || freeSlots.empty()) {
                     for (int64_t i = b - 1; i >= a; --i) {
-                        R.restore(tp->slot(slot));
+                        restore_at(slot, a);
                         advance(i - a);
                         rev_at_R(i);
                     }
                     return;
                 }
                 const int64_t m = plan_split(b - a, c);
-                R.restore(tp->slot(slot));
+                restore_at(slot, a);
                 advance(m);
                 const int ns = freeSlots.back();
                 freeSlots.pop_back();
@@ -1335,6 +1390,7 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
             freeSlots.push_back(taken[k].second);
         }
     }
+    flush_theta(*S);
     SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gX[gcur].p, outX.p);
     SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gV[gcur].p, outV.p);
     haveResult = true;

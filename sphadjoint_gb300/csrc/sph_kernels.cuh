@@ -701,26 +701,25 @@ __global__ void __launch_bounds__(kBlock)
     }
 }
 
-// Per design node: gtheta += this step's exact sum; clear the accumulator.
-// Threads n < B also reset the exponent slot the next step will use.
+// Per design node: gtheta += one step's exact sum; clear the accumulator.
+// Threads n < B also reset the exponent slot the following step will use.
 template <typename T>
-__global__ void k_theta_node(int64_t nnode, int B, const Inst<T> *__restrict__ inst,
-                             unsigned long long *__restrict__ acc, int *__restrict__ emax,
-                             int parity, double *__restrict__ gtheta)
+__device__ __forceinline__ void theta_node(int64_t n, int64_t nnode, int B,
+                                           const Inst<T> *__restrict__ inst,
+                                           unsigned long long *__restrict__ acc,
+                                           int *__restrict__ emax, int parity,
+                                           double *__restrict__ gtheta)
 {
-    const int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnode) return;
     unsigned long long lo = acc[2 * n], hi = acc[2 * n + 1];
-    const bool any = (lo | hi) != 0ull;
-    int b = 0;
-    if (any) {
+    if ((lo | hi) != 0ull) {
         // instance owning node n (design-node offsets are increasing)
         int lo_b = 0, hi_b = B - 1;
         while (lo_b < hi_b) {
             const int mid = (lo_b + hi_b + 1) >> 1;
             if (inst[mid].toff <= n) lo_b = mid; else hi_b = mid - 1;
         }
-        b = lo_b;
+        const int b = lo_b;
         const int em = emax[2 * b + parity];
         acc[2 * n] = 0ull;
         acc[2 * n + 1] = 0ull;
@@ -734,6 +733,39 @@ __global__ void k_theta_node(int64_t nnode, int B, const Inst<T> *__restrict__ i
         gtheta[n] += ldexp(vv, -theta_scale(em, inst[b].lgN));
     }
     if (n < B) emax[2 * n + (1 - parity)] = INT_MIN;
+}
+
+template <typename T>
+__global__ void k_theta_node(int64_t nnode, int B, const Inst<T> *__restrict__ inst,
+                             unsigned long long *__restrict__ acc, int *__restrict__ emax,
+                             int parity, double *__restrict__ gtheta)
+{
+    theta_node<T>((int64_t)blockIdx.x * blockDim.x + threadIdx.x, nnode, B, inst, acc, emax,
+                  parity, gtheta);
+}
+
+// _tape_load! of the next reverse step fused with the design-node write-back
+// of the previous one: the first gridN blocks gather, the rest flush nodes.
+template <typename T>
+__global__ void k_gather_theta(int64_t N, unsigned gridN, const int32_t *__restrict__ perm,
+                               const int32_t *__restrict__ srcInv, const T2<T> *__restrict__ sx,
+                               const T2<T> *__restrict__ sv, T2<T> *__restrict__ pos,
+                               T2<T> *__restrict__ vel, int64_t nnode, int B,
+                               const Inst<T> *__restrict__ inst,
+                               unsigned long long *__restrict__ acc, int *__restrict__ emax,
+                               int parity, double *__restrict__ gtheta)
+{
+    if (blockIdx.x < gridN) {
+        const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (t >= N) return;
+        int32_t s = perm[t];
+        if (srcInv) s = srcInv[s];
+        pos[t] = sx[s];
+        vel[t] = sv[s];
+    } else {
+        theta_node<T>((int64_t)(blockIdx.x - gridN) * blockDim.x + threadIdx.x, nnode, B, inst,
+                      acc, emax, parity, gtheta);
+    }
 }
 
 template <typename T>
