@@ -72,6 +72,57 @@ def workload(n_side=1024, nsteps=1000, snapshots=32, ntheta=256, dtype="f32"):
     return p, X0, V0, theta, cfg
 
 
+def small_workload():
+    """The reference's CPU-runnable dam break: a 56 x 37 block (2072 particles),
+    dx = 0.01, origin (dx, dx), 1.6 x 1.0 tank, h = 1.3 dx, rho0 = 1000,
+    c0 = 10 sqrt(2 g H), mu = 0.02, kw = 5e4, dt = 0.25 h / c0, theta 32 x 32 of
+    zeros, 5333 steps in FP64 with a full tape."""
+    dx, nx, ny = 0.01, 56, 37
+    H = ny * dx
+    h = 1.3 * dx
+    c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+    p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0, Lx=1.6,
+             Ly=1.0, kw=5e4, ngx=32, ngy=32)
+    xs = dx + dx * np.arange(nx)
+    ys = dx + dx * np.arange(ny)
+    X, Y = np.meshgrid(xs, ys)
+    X0 = np.vstack([X.ravel(), Y.ravel()])
+    cfg = {"workload": "small dam break: 56x37 = 2072 particles, 5333 steps FP64, full tape, "
+                       "theta 32x32 zeros", "particles": nx * ny, "time_steps": 5333,
+           "snapshots": 0, "theta": [32, 32], "tank": [1.6, 1.0], "dx": dx, "skin": 0.2,
+           "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half"}
+    return p, X0, np.zeros_like(X0), np.zeros((32, 32)), cfg
+
+
+def dense_workload(side=2896, ntheta=512, seed=5):
+    """Dense stress case: a side x side block (8,386,816 particles for 2896)
+    compressed 1.15x (spacing dx/1.15 with the mass of the uncompressed
+    lattice), rebuilt every step, 200 steps, 16 checkpoints, theta 512 x 512
+    with 50% solid cells in seeded random blobs (alpha 1000 vs 0)."""
+    dx = 1e-3
+    sp = dx / 1.15
+    H = side * sp
+    h = 1.3 * dx
+    c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+    p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0,
+             Lx=2.0 * H, Ly=1.25 * H, kw=5e4, ngx=ntheta, ngy=ntheta)
+    rng = np.random.default_rng(seed)
+    xs = sp + sp * np.arange(side)
+    X, Y = np.meshgrid(xs, xs)
+    X0 = np.vstack([X.ravel(), Y.ravel()]) + rng.uniform(-0.05 * sp, 0.05 * sp, (2, side * side))
+    f = rng.standard_normal((ntheta, ntheta))
+    for _ in range(6):  # blobs: repeated 5x5 box smoothing
+        pad = np.pad(f, 2, mode="wrap")
+        f = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
+    theta = np.where(f > np.median(f), 1000.0, 0.0)
+    cfg = {"workload": f"dense stress: {side}x{side} = {side * side} particles compressed 1.15x, "
+                       "rebuilt every step, 200 steps FP32, 16 checkpoints, theta 512x512 "
+                       "with 50% solid blobs", "particles": side * side, "time_steps": 200,
+           "snapshots": 16, "theta": [ntheta, ntheta], "dx": sp, "skin": 0.2, "interval": 1,
+           "maxnb": 64, "objective": "kinetic energy, right half"}
+    return p, X0, np.zeros_like(X0), theta, cfg
+
+
 def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3):
     """64 independent dam breaks: N log-uniform in [1k, 64k], aspect (height /
     width of the water block) uniform in [0.3, 1.0], each with its own seeded,
@@ -368,7 +419,7 @@ def dist_info():
     return ws, rank, local
 
 
-def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64):
+def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64, interval=4):
     """Time the oracle (forward + adjoint with a full tape) on all host cores
     on the first few time steps of the workload; returns particle-steps/s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -382,7 +433,7 @@ def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64):
     N = X0.shape[1]
 
     def run(nsteps):
-        st = o.state(op, X0, V0)
+        st = o.state(op, X0, V0, interval=interval)
         tp = o.tape(N, nsteps)
         t0 = time.perf_counter()
         o.simulate(st, th, op, nsteps, tp)
@@ -390,7 +441,7 @@ def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64):
         right = X[:, 0] > p["Lx"] / 2
         sV = np.where(right[:, None], p["m"] * V, 0.0)
         ws = o.workspace(N, op)
-        o.backward(ws, tp, th, op, np.zeros_like(X), sV)
+        o.backward(ws, tp, th, op, np.zeros_like(X), sV, interval=interval)
         return time.perf_counter() - t0
 
     t1 = run(1)
@@ -447,13 +498,21 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
 
-    p_d, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
-                                       args.dtype)
+    interval = 4
+    if args.workload == "small":
+        p_d, X0, V0, theta, cfg = small_workload()
+        args.dtype, args.nsteps, args.snapshots = "f64", 5333, 0
+    elif args.workload == "dense":
+        p_d, X0, V0, theta, cfg = dense_workload()
+        args.nsteps, args.snapshots, interval = 200, 16, 1
+    else:
+        p_d, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
+                                           args.dtype)
     p = S.SPHParams(**p_d, dtype=args.dtype)
     N = X0.shape[1]
     pc = p.c_struct()
-    st0 = S.State(X0, V0, p)             # pristine initial state (device)
-    st = S.State(X0, V0, p)
+    st0 = S.State(X0, V0, p, interval=interval)  # pristine initial state (device)
+    st = S.State(X0, V0, p, interval=interval)
     th = S.DesignField(theta, args.dtype)
     tape = S.Tape(N, args.nsteps, p, snapshots=args.snapshots)
     ws = S.AdjointWorkspace(N, p)
@@ -465,7 +524,7 @@ def run_ours(args):
         tape.reset()
         LB.check(L.sph_simulate(st.h, th.h, C.byref(pc), args.nsteps, tape.h, C.byref(flags)))
         LB.check(L.sph_objective(ws.h, st.h, 0, None, C.byref(pc), C.byref(J)))
-        LB.check(L.sph_backward_seeded(ws.h, tape.h, th.h, C.byref(pc), None, 0.2, 4, 64,
+        LB.check(L.sph_backward_seeded(ws.h, tape.h, th.h, C.byref(pc), None, 0.2, interval, 64,
                                        C.byref(flags)))
 
     blocks = None
@@ -554,7 +613,7 @@ def run_ours(args):
         def solve_host():
             h = C.c_void_p()
             LB.check(L.sph_state_create(C.byref(pc), N, Xh.ctypes.data_as(C.c_void_p),
-                                        Vh.ctypes.data_as(C.c_void_p), p.code, 0.2, 4, 64,
+                                        Vh.ctypes.data_as(C.c_void_p), p.code, 0.2, interval, 64,
                                         C.byref(h)))
             LB.check(L.sph_field_upload(th.h, thh.ctypes.data_as(C.c_void_p)))
             tape.reset()
@@ -564,7 +623,7 @@ def run_ours(args):
             right = outX[:, 0] > p.Lx / 2
             sV = np.where(right[:, None], p.m * outV, 0).astype(p.np)
             LB.check(L.sph_backward(ws.h, tape.h, th.h, C.byref(pc), None,
-                                    sV.ctypes.data_as(C.c_void_p), None, 0.2, 4, 64,
+                                    sV.ctypes.data_as(C.c_void_p), None, 0.2, interval, 64,
                                     C.byref(flags)))
             LB.check(L.sph_workspace_get(ws.h, gX.ctypes.data_as(C.c_void_p),
                                          gV.ctypes.data_as(C.c_void_p),
@@ -586,7 +645,9 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
-        cpu = cpu_sample(p_d, X0, V0, theta, args.dtype, budget_s=args.cpu_seconds)
+        max_steps = args.nsteps if args.workload == "small" else 64
+        cpu = cpu_sample(p_d, X0, V0, theta, args.dtype, budget_s=args.cpu_seconds,
+                         max_steps=max_steps, interval=interval)
         cpu.pop("seconds", None)
 
     if rank == 0:
@@ -610,7 +671,8 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="single", choices=["single", "batched", "served"])
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "small", "dense", "batched", "served"])
     ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
     ap.add_argument("--rates", default="10,100,500", help="served: arrival rates (1/s)")
     ap.add_argument("--workers", type=int, default=6, help="served: concurrent requests")

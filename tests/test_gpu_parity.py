@@ -192,3 +192,26 @@ def test_autotuned_block_sizes_do_not_change_results():
     again = run_gpu(case, 10, seeds=seeds)
     for k in ("X", "V", "gX", "gV", "gtheta"):
         assert np.array_equal(ref[k], again[k]), k
+
+
+def test_small_dambreak_full_horizon_bit_exact():
+    """The reference's CPU case: 2072 particles, 5333 steps in FP64, KE of the
+    right half. J, the final state and dJ/dX0, dJ/dV0 stay bit-identical to the
+    oracle over the whole horizon (same summation order, no FMA); repeated
+    runs give the same J (the reference's determinism claim)."""
+    case = K.dambreak_case(theta_seed=21)
+    case["theta"] = case["theta"] * 0.1
+    p = case["p"]
+    seeds = lambda X, V: K.ke_seeds(X, V, p)[1:]  # noqa: E731
+    n = 5333
+    g = run_gpu(case, n, seeds=seeds)
+    r = run_oracle(case, n, seeds=seeds)
+    assert g["flags"] == r["flags"] and g["bflags"] == r["bflags"]
+    assert np.array_equal(g["X"], r["X"]) and np.array_equal(g["V"], r["V"])
+    Jg = K.ke_seeds(g["X"], g["V"], p)[0]
+    Jr = K.ke_seeds(r["X"], r["V"], p)[0]
+    assert Jg == Jr and Jg > 0
+    assert np.array_equal(g["gX"], r["gX"]) and np.array_equal(g["gV"], r["gV"])
+    assert K.relerr(g["gtheta"], r["gtheta"]) <= 1e-12
+    g2 = run_gpu(case, n, seeds=seeds)
+    assert np.array_equal(g2["X"], g["X"]) and np.array_equal(g2["gtheta"], g["gtheta"])
