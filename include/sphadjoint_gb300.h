@@ -200,7 +200,10 @@ SPH_API int32_t sph_batch_objective(sph_workspace ws, sph_state st, int32_t kind
    others run and their kernels overlap on the device. Each result equals the
    same request solved alone. Host inputs of a request (X0, V0, theta) must
    stay valid, and its outputs (gX, gV, gtheta; any may be NULL) are written,
-   before sph_server_wait returns. Wait for every ticket before destroying. */
+   before sph_server_wait returns. A request whose gX, gV and gtheta are all
+   NULL is forward only (objective_only in scripts/03_optimize.jl:248-254):
+   no tape and no reverse sweep, J alone. Wait for every ticket before
+   destroying. */
 typedef struct sph_server_s *sph_server;
 typedef struct sph_request {
     sph_params p;

@@ -54,6 +54,8 @@ int64_t request_bytes(const sph_request &r, int dtype)
     const int64_t cells = (int64_t)((r.p.Lx / rc + 3) * (r.p.Ly / rc + 3));
     const int64_t nodes = (int64_t)r.p.ngx * r.p.ngy;
     int64_t tape;
+    if (!r.gX && !r.gV && !r.gtheta)
+        return state + work + 8 * cells + 40 * nodes + (16 << 20);   // forward only
     if (r.snapshots > 0)
         tape = (int64_t)r.snapshots * (N * (6 * s + 40) + 4 * cells) + state;
     else
@@ -236,8 +238,12 @@ class Server {
                                            : make_state_f32(ps, ns, r.X0, r.V0, o));
             std::unique_ptr<FieldI> th(f64 ? make_field_f64(gx, gy, r.theta)
                                            : make_field_f32(gx, gy, r.theta));
-            std::unique_ptr<TapeI> tp(f64 ? make_tape_f64(r.N, r.nsteps, r.snapshots)
-                                          : make_tape_f32(r.N, r.nsteps, r.snapshots));
+            // no output buffers: a forward-only request (no tape, no reverse sweep)
+            const bool adjoint = r.gX || r.gV || r.gtheta;
+            std::unique_ptr<TapeI> tp;
+            if (adjoint)
+                tp.reset(f64 ? make_tape_f64(r.N, r.nsteps, r.snapshots)
+                             : make_tape_f32(r.N, r.nsteps, r.snapshots));
             std::unique_ptr<WorkI> ws(f64 ? make_work_f64(ps, ns) : make_work_f32(ps, ns));
             st->simulate(th.get(), nullptr, r.nsteps, tp.get());
             uint32_t f = st->take_flags();
@@ -245,8 +251,10 @@ class Server {
             ws->objective(st.get(), r.objective, r.objective == SPH_OBJ_TARGET ? r.obj_args : nullptr,
                           nullptr, &J);
             uint32_t fb = 0;
-            ws->backward_seeded(tp.get(), th.get(), &p, nullptr, o, &fb);
-            ws->get(r.gX, r.gV, r.gtheta);
+            if (adjoint) {
+                ws->backward_seeded(tp.get(), th.get(), &p, nullptr, o, &fb);
+                ws->get(r.gX, r.gV, r.gtheta);
+            }
             q.J = J;
             q.flags = f | fb;
             return true;

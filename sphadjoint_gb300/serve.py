@@ -22,16 +22,20 @@ class Ticket:
     """One submitted request: keeps its host inputs alive and owns its outputs."""
 
     def __init__(self, server, p, X0, V0, theta, nsteps, snapshots, objective, args, skin,
-                 interval, maxnb):
+                 interval, maxnb, adjoint=True):
         self.server = server
         N = int(np.asarray(X0).size // 2)
         self.N, self.p, self.nsteps = N, p, int(nsteps)
         self._x = _xy(X0, N, p.np)
         self._v = _xy(V0, N, p.np)
         self._th = np.asfortranarray(np.asarray(theta, dtype=p.np))
-        self.gX = np.empty((N, 2), p.np)
-        self.gV = np.empty((N, 2), p.np)
-        self.gt = np.empty((p.ngx, p.ngy), p.np)
+        self.adjoint = bool(adjoint)
+        if self.adjoint:
+            self.gX = np.empty((N, 2), p.np)
+            self.gV = np.empty((N, 2), p.np)
+            self.gt = np.empty((p.ngx, p.ngy), p.np)
+        else:  # forward only: J alone, no tape and no reverse sweep
+            self.gX = self.gV = self.gt = None
         r = L.sph_request()
         r.p = p.c_struct()
         r.N = N
@@ -55,8 +59,9 @@ class Ticket:
             J, lat, f = C.c_double(), C.c_double(), C.c_uint32()
             L.check(self.server._L.sph_server_wait(self.server.h, self.ticket, C.byref(J),
                                                    C.byref(lat), C.byref(f)))
-            self.result = dict(J=J.value, latency_ms=lat.value, flags=f.value, gX=self.gX.T,
-                               gV=self.gV.T, gtheta=self.gt.T)
+            self.result = dict(J=J.value, latency_ms=lat.value, flags=f.value)
+            if self.adjoint:
+                self.result.update(gX=self.gX.T, gV=self.gV.T, gtheta=self.gt.T)
         return self.result
 
     def done(self) -> bool:
@@ -76,11 +81,12 @@ class Server:
         self.tickets = []
 
     def submit(self, p: SPHParams, X0, V0, theta, nsteps, snapshots=0, objective="ke_right",
-               args=None, skin=0.2, interval=4, maxnb=64) -> Ticket:
+               args=None, skin=0.2, interval=4, maxnb=64, adjoint=True) -> Ticket:
+        """Queue one solve. adjoint=False: forward only, the result holds J alone."""
         if p.dtype != self.dtype:
             raise ValueError("request dtype differs from the server's")
         t = Ticket(self, p, X0, V0, theta, nsteps, snapshots, objective, args, skin, interval,
-                   maxnb)
+                   maxnb, adjoint)
         self.tickets.append(t)
         return t
 
