@@ -267,6 +267,18 @@ SPH_API int32_t sph_build_cells_noalloc(const void *X_dev, int64_t N, int32_t dt
    positions and velocities are not changed. */
 SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_t *blocks);
 
+/* Lanes per particle of the neighbour-list and pair-sum kernels (no
+   counterpart in the reference), process-wide. 0 (default): by state size --
+   FP64 single states of up to 16384 particles give each particle a group of
+   32 lanes (up to 512 particles) or 16 lanes, everything else one thread.
+   1: always one thread. 16 or 32: groups for every single-instance state.
+   Every setting adds each particle's pair terms in the same order, so FP64
+   results are bit-identical across settings; FP32 results may differ in the
+   last bits (multiply-add contraction differs between the forms). Batches
+   always use one thread per particle. Other values: SPH_ERR_ARG. */
+SPH_API int32_t sph_set_group_lanes(int32_t lanes);
+SPH_API int32_t sph_get_group_lanes(int32_t *lanes);
+
 /* ---- instrumentation ---- */
 /* kernels launched by this library since load */
 SPH_API int64_t sph_launch_count(void);

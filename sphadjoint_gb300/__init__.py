@@ -15,9 +15,11 @@ from .api import (  # noqa: F401
     backward,
     build,
     build_neighbors,
+    group_lanes,
     kinetic_energy_right_half,
     launch_count,
     reset,
+    set_group_lanes,
     simulate,
     step,
     synchronize,

@@ -95,6 +95,8 @@ _SIGS = {
     "sph_workspace_get": (_I32, [_P, _P, _P, _P]),
     "sph_state_assign": (_I32, [_P, _P]),
     "sph_autotune": (_I32, [_P, _P, _I32, _I32P]),
+    "sph_set_group_lanes": (_I32, [_I32]),
+    "sph_get_group_lanes": (_I32, [_I32P]),
     "sph_objective": (_I32, [_P, _P, _I32, _DP, _SP, _DP]),
     "sph_backward_seeded": (_I32, [_P, _P, _P, _SP, _P, C.c_double, _I32, _I32, _U32P]),
     "sph_batch_create": (_I32, [_I32, _SP, _I64P, _P, _P, _I32, C.c_double, _I32, _I32, _PP]),

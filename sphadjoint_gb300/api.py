@@ -513,3 +513,17 @@ def launch_count() -> int:
 
 def synchronize():
     L.check(L.load().sph_synchronize())
+
+
+def set_group_lanes(lanes: int) -> None:
+    """Lanes per particle of the pair-sum kernels, process-wide (no counterpart
+    in the reference): 0 = by state size (default), 1 = one thread per
+    particle, 16 or 32 = a lane group per particle for single states. FP64
+    results are bit-identical across settings."""
+    L.check(L.load().sph_set_group_lanes(int(lanes)))
+
+
+def group_lanes() -> int:
+    v = C.c_int32()
+    L.check(L.load().sph_get_group_lanes(C.byref(v)))
+    return v.value

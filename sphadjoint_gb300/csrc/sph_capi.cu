@@ -23,6 +23,7 @@ thread_local std::string g_err;
 thread_local cudaStream_t g_stream = nullptr;
 thread_local bool g_stream_external = false;
 std::atomic<long long> g_launches{0};
+std::atomic<int> g_group_lanes{0};
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {};
 
@@ -113,6 +114,9 @@ void rt_after_launch(int kid)
 }
 
 void rt_check_launch(const char *name) { cuda_check(cudaGetLastError(), name); }
+
+int rt_group_lanes() { return g_group_lanes.load(std::memory_order_relaxed); }
+void rt_set_group_lanes(int lanes) { g_group_lanes.store(lanes, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
 // Binomial checkpointing (Griewank's revolve bound). With c snapshot slots and
@@ -477,6 +481,23 @@ SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_
         ST(st)->autotune(FD(theta), reps, b);
         if (blocks)
             for (int k = 0; k < 6; ++k) blocks[k] = b[k];
+    });
+}
+
+SPH_API int32_t sph_set_group_lanes(int32_t lanes)
+{
+    return guarded([&] {
+        if (lanes != 0 && lanes != 1 && lanes != 16 && lanes != 32)
+            throw Error(ERR_ARG, "lanes per particle must be 0, 1, 16 or 32");
+        rt_set_group_lanes(lanes);
+    });
+}
+
+SPH_API int32_t sph_get_group_lanes(int32_t *lanes)
+{
+    return guarded([&] {
+        need(lanes, "lanes");
+        *lanes = rt_group_lanes();
     });
 }
 

@@ -22,6 +22,7 @@
 #include <utility>
 #include <vector>
 
+#include "sph_coop.cuh"
 #include "sph_iface.hpp"
 #include "sph_kernels.cuh"
 
@@ -119,6 +120,29 @@ template <typename T> int &tuned_block(int kid, bool multi)
             ::sphgb::rt_after_launch(kid);                                                    \
         }                                                                                     \
     } while (0)
+
+// Group-per-particle launch: kCoopBlock threads, kCoopBlock / G particles per
+// block.
+#define SPH_LAUNCH_COOP(kid, G, kern, n, ...)                                                \
+    do {                                                                                      \
+        if ((n) > 0) {                                                                        \
+            const int per_ = ::sphgb::kCoopBlock / (G);                                       \
+            ::sphgb::rt_before_launch(kid);                                                   \
+            kern<<<(unsigned)(((n) + per_ - 1) / per_), ::sphgb::kCoopBlock, 0,               \
+                   ::sphgb::rt_stream()>>>(__VA_ARGS__);                                      \
+            ::sphgb::rt_after_launch(kid);                                                    \
+        }                                                                                     \
+    } while (0)
+
+// FP64 single states up to this many particles use lane groups by default:
+// one thread per particle would leave most SMs idle on the slow FP64 pipe.
+// Kernel time per fwd+adjoint step (density .. pass 2), one thread / 16 /
+// 32 lanes: 240 particles 538 / 112 / 100 us, 1024: 560 / 112 / 123 us,
+// 2072: 110 (pass 1 alone) / 30 / 42 us, 8288: 555 / 346 / 501 us. 32 lanes
+// win only for a few hundred particles, where the critical path of one
+// group matters more than the total work.
+constexpr int64_t kCoopMaxN = 16384;
+constexpr int64_t kCoop32MaxN = 512;
 
 // Constants formed in T exactly as the reference kernels form them.
 template <typename T> Phys<T> make_phys(const Params &q)
@@ -396,6 +420,16 @@ template <typename T> class Sys final : public StateI {
     int64_t N() const override { return N_; }
     int batch() const override { return B; }
 
+    // lanes per particle of this state's pair-sum kernels (0: one thread)
+    int group_lanes() const
+    {
+        if (B != 1) return 0;
+        const int f = rt_group_lanes();
+        if (f == 16 || f == 32) return f;
+        if (f == 1 || sizeof(T) != 8 || N_ > kCoopMaxN) return 0;
+        return N_ <= kCoop32MaxN ? 32 : 16;
+    }
+
     void upload_inst()
     {
         SPH_CK(cudaMemcpyAsync(dinst.p, hinst.data(), sizeof(Inst<T>) * B, cudaMemcpyHostToDevice, rt_stream()));
@@ -539,9 +573,15 @@ template <typename T> class Sys final : public StateI {
                        bucketId.p, pos[cur].p, vel[cur].p, pos[nxt].p, vel[nxt].p, xref.p, perm.p,
                        invperm.p, ex0, ex0N, ex1, ex1N);
             cur = nxt;
-            auto kn = B > 1 ? &k_nl_build<T, true> : &k_nl_build<T, false>;
-            SPH_LAUNCH_TUNED(K_NLBUILD, B > 1, kn, N_, N_, hinst[0], dinst.p, pinst.p, pos[cur].p,
-                             cellStart.p, center.p, masks.p, nbcount.p, flags.p);
+            if (const int G = group_lanes()) {
+                auto kn = G == 32 ? &k_nl_build_coop<T, 32> : &k_nl_build_coop<T, 16>;
+                SPH_LAUNCH_COOP(K_NLBUILD, G, kn, N_, N_, hinst[0], pos[cur].p, cellStart.p,
+                                center.p, masks.p, nbcount.p, flags.p);
+            } else {
+                auto kn = B > 1 ? &k_nl_build<T, true> : &k_nl_build<T, false>;
+                SPH_LAUNCH_TUNED(K_NLBUILD, B > 1, kn, N_, N_, hinst[0], dinst.p, pinst.p,
+                                 pos[cur].p, cellStart.p, center.p, masks.p, nbcount.p, flags.p);
+            }
         }
         age = 0;
         cellsOnlyLatest = false;
@@ -599,14 +639,24 @@ template <typename T> class Sys final : public StateI {
         if (N_ == 0) return;
         if (tx) SPH_LAUNCH(K_TAPE, k_tape_store<T>, N_, N_, perm.p, pos[cur].p, vel[cur].p, tx, tv);
         NLView<T> v = view();
-        auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
-        SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rho.p, prho.p, tmask.p);
-        v.tmask = tmask.p;
         const int nxt = 1 - cur;
-        auto ki = B > 1 ? &k_accel_integrate<T, true> : &k_accel_integrate<T, false>;
-        SPH_LAUNCH_TUNED(K_ACCEL_INTEGRATE, B > 1, ki, N_, v, vel[cur].p, prho.p, theta,
-                         pos[nxt].p, vel[nxt].p, keepAccel ? accOut.p : (T2<T> *)nullptr,
-                         keepAccel ? alphaOut.p : (T *)nullptr, flags.p);
+        T2<T> *aO = keepAccel ? accOut.p : (T2<T> *)nullptr;
+        T *alO = keepAccel ? alphaOut.p : (T *)nullptr;
+        if (const int G = group_lanes()) {
+            auto kd = G == 32 ? &k_density_eos_coop<T, 32> : &k_density_eos_coop<T, 16>;
+            SPH_LAUNCH_COOP(K_DENSITY, G, kd, N_, v, rho.p, prho.p, tmask.p);
+            v.tmask = tmask.p;
+            auto ki = G == 32 ? &k_accel_integrate_coop<T, 32> : &k_accel_integrate_coop<T, 16>;
+            SPH_LAUNCH_COOP(K_ACCEL_INTEGRATE, G, ki, N_, v, vel[cur].p, prho.p, theta,
+                            pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
+        } else {
+            auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
+            SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rho.p, prho.p, tmask.p);
+            v.tmask = tmask.p;
+            auto ki = B > 1 ? &k_accel_integrate<T, true> : &k_accel_integrate<T, false>;
+            SPH_LAUNCH_TUNED(K_ACCEL_INTEGRATE, B > 1, ki, N_, v, vel[cur].p, prho.p, theta,
+                             pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
+        }
         cur = nxt;
     }
 
@@ -1039,6 +1089,23 @@ template <typename T> class Work final : public WorkI {
         if (did) gcur = g2;
         NLView<T> v = S.view();
         const T2<T> *vel = S.vel[S.cur].p;
+        if (const int G = S.group_lanes()) {
+            const bool g32 = G == 32;
+            auto kd = g32 ? &k_density_eos_coop<T, 32> : &k_density_eos_coop<T, 16>;
+            auto ka = g32 ? &k_accel_drag_adj_coop<T, 32> : &k_accel_drag_adj_coop<T, 16>;
+            auto k1 = g32 ? &k_pass1_design_coop<T, 32> : &k_pass1_design_coop<T, 16>;
+            auto k2 = g32 ? &k_pass2_axpy_coop<T, 32> : &k_pass2_axpy_coop<T, 16>;
+            SPH_LAUNCH_COOP(K_DENSITY, G, kd, N_, v, (T *)nullptr, S.prho.p, S.tmask.p);
+            v.tmask = S.tmask.p;
+            SPH_LAUNCH_COOP(K_ACCEL_DRAG, G, ka, N_, v, vel, S.prho.p, theta, gX[gcur].p,
+                            gV[gcur].p, abar.p, galpha.p, emax.p, parity);
+            SPH_LAUNCH_COOP(K_PASS1, G, k1, N_, v, vel, S.prho.p, theta, abar.p, galpha.p, gXs.p,
+                            grho.p, gV[gcur].p);
+            SPH_LAUNCH_COOP(K_PASS2, G, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p,
+                            parity, thetaAcc.p);
+            pendingTheta = parity;
+            return;
+        }
         const bool multi = S.B > 1;
         auto kd = multi ? &k_density_eos<T, true> : &k_density_eos<T, false>;
         auto ka = multi ? &k_accel_drag_adj<T, true> : &k_accel_drag_adj<T, false>;

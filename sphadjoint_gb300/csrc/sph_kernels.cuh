@@ -275,6 +275,131 @@ __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restri
 // integrate_kernel! (fused; positions and velocities double-buffered because
 // neighbours read the pre-step state).
 // ---------------------------------------------------------------------------
+// Per-pair terms, shared by the thread-per-particle kernels and the
+// group-per-particle kernels (sph_coop.cuh): each kernel adds them into its
+// running sums in slot order, so both forms round identically.
+
+// density_kernel!: m W(r) = m (A u^4 (2q + 1)).
+template <typename T>
+__device__ __forceinline__ T density_pair(T r2, T invh, T m, T A)
+{
+    const T q = pair_sqrt(r2) * invh;
+    const T u = (T)1 - (T)0.5 * q;
+    const T u2 = u * u;
+    return m * (A * u2 * u2 * ((T)2 * q + (T)1));
+}
+
+// accel_kernel!: a_i -= P F d, then a_i += C (v_i - v_j), per component.
+template <typename T> struct AccelPair {
+    T px, py, cx, cy;
+};
+template <typename T>
+__device__ __forceinline__ AccelPair<T> accel_pair(T r2, T dx, T dy, T invh, T m, T Fc,
+                                                   T twomumass, T pti, T iri, const T2<T> &vi,
+                                                   const T2<T> &pj, const T2<T> &vj)
+{
+    const T q = pair_sqrt(r2) * invh;
+    const T u = (T)1 - (T)0.5 * q;
+    const T F = Fc * u * u * u;
+    const T Pij = m * (pti + pj.x);
+    AccelPair<T> o;
+    o.px = Pij * F * dx;
+    o.py = Pij * F * dy;
+    const T C = twomumass * iri * pj.y * F;
+    o.cx = C * (vi.x - vj.x);
+    o.cy = C * (vi.y - vj.y);
+    return o;
+}
+
+// adj_pass1_kernel!: gx -= P F da_x, gx += w d_x (same for y), gv += C da,
+// grho -= C ad_v ir_i, S += F ad_d.
+template <typename T> struct Pass1Pair {
+    T gxs, gxa, gys, gya, gvx, gvy, grs, sS;
+};
+template <typename T>
+__device__ __forceinline__ Pass1Pair<T> pass1_pair(T r2, T dx, T dy, T invh, T m, T Fc, T Gc,
+                                                   T twomumass, T pti, T iri, const T2<T> &vi,
+                                                   const T2<T> &ab, const T2<T> &pj,
+                                                   const T2<T> &abj, const T2<T> &vj)
+{
+    T r, rinv;
+    if constexpr (sizeof(T) == 4) {
+        rinv = r2 > (T)0 ? rsqrtf(r2) : (T)0;
+        r = r2 * rinv;
+    } else {
+        r = sqrt(r2);
+    }
+    const T q = r * invh;
+    const T u = (T)1 - (T)0.5 * q;
+    const T F = Fc * u * u * u;
+    const T G = Gc * u * u;
+    const T Pij = m * (pti + pj.x);
+    const T Cbase = twomumass * iri * pj.y;
+    const T C = Cbase * F;
+    const T dax = ab.x - abj.x;
+    const T day = ab.y - abj.y;
+    const T dvx = vi.x - vj.x;
+    const T dvy = vi.y - vj.y;
+    const T ad_d = -(dax * dx + day * dy);
+    const T ad_v = dax * dvx + day * dvy;
+    Pass1Pair<T> o;
+    o.gxs = Pij * F * dax;
+    o.gys = Pij * F * day;
+    const T Fbar = Pij * ad_d + Cbase * ad_v;
+    T w;
+    if constexpr (sizeof(T) == 4) w = Fbar * G * invh * rinv;
+    else w = Fbar * G * invh / r;
+    o.gxa = w * dx;
+    o.gya = w * dy;
+    o.gvx = C * dax;
+    o.gvy = C * day;
+    o.grs = C * ad_v * iri;
+    o.sS = F * ad_d;
+    return o;
+}
+
+// adj_pass2_kernel!: gx += w d, w = m F (grho_i + grho_j).
+template <typename T>
+__device__ __forceinline__ T pass2_weight(T r2, T invh, T m, T Fc, T gri, T grj)
+{
+    const T q = pair_sqrt(r2) * invh;
+    const T u = (T)1 - (T)0.5 * q;
+    return m * (Fc * u * u * u) * (gri + grj);
+}
+
+// Density sum of a spilled particle (rows longer than 64 slots): the generic
+// neighbour walk; its in-support words are all zero (later passes walk it the
+// same way).
+template <typename T, typename IT>
+__device__ __forceinline__ T density_spill_sum(const NLView<T> &v, const IT &I, int64_t i,
+                                               const T2<T> &xi, uint32_t *__restrict__ tmaskOut)
+{
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, A = I.p.A;
+    T acc = (T)0;
+    for_each_neighbor<T>(v, I, i, [&](int j) {
+        const T2<T> xj = v.pos[j];
+        const T dx = xi.x - xj.x;
+        const T dy = xi.y - xj.y;
+        const T r2 = dx * dx + dy * dy;
+        if (r2 < r2max) acc += density_pair<T>(r2, invh, m, A);
+    });
+    if (tmaskOut)
+        for (int w = 0; w < 6; ++w) tmaskOut[(int64_t)w * v.N + i] = 0u;
+    return acc;
+}
+
+// Self term and eos_kernel!: rho = sum + m A, pterm = c^2 (rho - rho0) / rho^2.
+template <typename T, typename IT>
+__device__ __forceinline__ void density_finish(const IT &I, int64_t i, T acc, T *__restrict__ rho,
+                                               T2<T> *__restrict__ prho)
+{
+    const T m = I.p.m, A = I.p.A;
+    const T ri = acc + m * A;
+    if (rho) rho[i] = ri;
+    const T inv = (T)1 / ri;
+    prho[i] = mk2<T>(I.p.c2 * (ri - I.p.rho0) * inv * inv, inv);
+}
+
 // density_kernel! + eos_kernel!. It also records, for the rest of this step,
 // which neighbour-list entries are inside the support (r^2 < 4h^2): the later
 // passes of the step walk only those (same set, same order), skipping the
@@ -325,32 +450,13 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
             const T r2 = dx * dx + dy * dy;
             if (r2 < r2max) {
                 tw |= 1u << k;
-                const T q = pair_sqrt(r2) * invh;
-                const T u = (T)1 - (T)0.5 * q;
-                const T u2 = u * u;
-                acc += m * (A * u2 * u2 * ((T)2 * q + (T)1));
+                acc += density_pair<T>(r2, invh, m, A);
             }
         }
     } else {
-        for_each_neighbor<T>(v, I, i, [&](int j) {
-            const T2<T> xj = v.pos[j];
-            const T dx = xi.x - xj.x;
-            const T dy = xi.y - xj.y;
-            const T r2 = dx * dx + dy * dy;
-            if (r2 < r2max) {
-                const T q = pair_sqrt(r2) * invh;
-                const T u = (T)1 - (T)0.5 * q;
-                const T u2 = u * u;
-                acc += m * (A * u2 * u2 * ((T)2 * q + (T)1));
-            }
-        });
-        if (tmaskOut)
-            for (int w = 0; w < 6; ++w) tmaskOut[(int64_t)w * v.N + i] = 0u;
+        acc = density_spill_sum<T>(v, I, i, xi, tmaskOut);
     }
-    const T ri = acc + m * A;
-    if (rho) rho[i] = ri;
-    const T inv = (T)1 / ri;
-    prho[i] = mk2<T>(I.p.c2 * (ri - I.p.rho0) * inv * inv, inv);
+    density_finish<T>(I, i, acc, rho, prho);
 }
 
 // Pressure + Morris viscosity (accel_kernel! pair loop).
@@ -371,20 +477,21 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < r2max) {
-            const T q = pair_sqrt(r2) * invh;
-            const T u = (T)1 - (T)0.5 * q;
-            const T F = Fc * u * u * u;
-            const T2<T> pj = prho[j];
-            const T Pij = m * (pti + pj.x);
-            ax -= Pij * F * dx;
-            ay -= Pij * F * dy;
-            const T C = twomumass * iri * pj.y * F;
-            const T2<T> vj = vel[j];
-            ax += C * (vi.x - vj.x);
-            ay += C * (vi.y - vj.y);
+            const AccelPair<T> t =
+                accel_pair<T>(r2, dx, dy, invh, m, Fc, twomumass, pti, iri, vi, prho[j], vel[j]);
+            ax -= t.px;
+            ay -= t.py;
+            ax += t.cx;
+            ay += t.cy;
         }
     });
 }
+
+template <typename T, typename IT>
+__device__ __forceinline__ void accel_integrate_finish(
+    const IT &I, int b, int64_t i, const T2<T> &xi, const T2<T> &vi, T ax, T ay,
+    const T *__restrict__ theta, T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
+    T2<T> *__restrict__ aOut, T *__restrict__ alphaOut, uint32_t *__restrict__ flags);
 
 // accel_kernel! (pressure + viscosity + gravity + wall, and alpha) fused with
 // integrate_kernel! (semi-implicit Euler, implicit Brinkman drag).
@@ -404,6 +511,16 @@ __global__ void __launch_bounds__(kBlock)
     const T2<T> vi = vel[i];
     T ax, ay;
     accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+    accel_integrate_finish<T>(I, b, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags);
+}
+
+// Gravity, wall, alpha and the integrator of one particle, after its pair sum.
+template <typename T, typename IT>
+__device__ __forceinline__ void accel_integrate_finish(
+    const IT &I, int b, int64_t i, const T2<T> &xi, const T2<T> &vi, T ax, T ay,
+    const T *__restrict__ theta, T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
+    T2<T> *__restrict__ aOut, T *__restrict__ alphaOut, uint32_t *__restrict__ flags)
+{
     const Phys<T> &p = I.p;
     const T al = interp_alpha_value<T>(theta + I.toff, xi.x, xi.y, p);
     ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
@@ -484,6 +601,35 @@ __global__ void k_gather_from_ids(int64_t N, const int32_t *__restrict__ perm,
 // Adjoint (gather form, src/adjoint.jl)
 // ---------------------------------------------------------------------------
 
+// _adj_integrate! + _adj_drag! of one particle after its recomputed pair sum;
+// returns the exponent bound of |galpha| (INT_MIN when it is zero).
+template <typename T, typename IT>
+__device__ __forceinline__ int drag_adj_finish(const IT &I, int64_t i, const T2<T> &xi,
+                                               const T2<T> &vi, T ax, T ay,
+                                               const T *__restrict__ theta,
+                                               const T2<T> *__restrict__ gX,
+                                               T2<T> *__restrict__ gV, T2<T> *__restrict__ abar,
+                                               T *__restrict__ galpha)
+{
+    const Phys<T> &p = I.p;
+    const T al = interp_alpha_value<T>(theta + I.toff, xi.x, xi.y, p);
+    ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
+    ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
+    const T dt = p.dt;
+    const T2<T> gx = gX[i];
+    T2<T> gv = gV[i];
+    gv.x += dt * gx.x;
+    gv.y += dt * gx.y;
+    const T D = (T)1 / ((T)1 + dt * al);
+    const T vx = (vi.x + dt * ax) * D;
+    const T vy = (vi.y + dt * ay) * D;
+    abar[i] = mk2<T>(dt * D * gv.x, dt * D * gv.y);
+    const T ga = -dt * D * (vx * gv.x + vy * gv.y);
+    galpha[i] = ga;
+    gV[i] = mk2<T>(D * gv.x, D * gv.y);
+    return (ga != (T)0 && isfinite(ga)) ? ilogb((double)ga) + 1 : INT_MIN; // |ga| < 2^e
+}
+
 // Accel recompute (accel_kernel!, for a_rest and alpha) + _adj_integrate!
 // (gV += dt gX) + _adj_drag! (implicit Brinkman VJP). Also records, per
 // instance, the largest binary exponent of |galpha| for the exact theta
@@ -507,23 +653,7 @@ __global__ void __launch_bounds__(kBlock)
         const T2<T> vi = vel[i];
         T ax, ay;
         accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
-        const Phys<T> &p = I.p;
-        const T al = interp_alpha_value<T>(theta + I.toff, xi.x, xi.y, p);
-        ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
-        ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
-        const T dt = p.dt;
-        const T2<T> gx = gX[i];
-        T2<T> gv = gV[i];
-        gv.x += dt * gx.x;
-        gv.y += dt * gx.y;
-        const T D = (T)1 / ((T)1 + dt * al);
-        const T vx = (vi.x + dt * ax) * D;
-        const T vy = (vi.y + dt * ay) * D;
-        abar[i] = mk2<T>(dt * D * gv.x, dt * D * gv.y);
-        const T ga = -dt * D * (vx * gv.x + vy * gv.y);
-        galpha[i] = ga;
-        gV[i] = mk2<T>(D * gv.x, D * gv.y);
-        if (ga != (T)0 && isfinite(ga)) e = ilogb((double)ga) + 1; // |ga| < 2^e
+        e = drag_adj_finish<T>(I, i, xi, vi, ax, ay, theta, gX, gV, abar, galpha);
     }
     // max over the lanes of each instance present in the warp, one atomic each
     const unsigned act = __ballot_sync(0xffffffffu, live);
@@ -537,6 +667,21 @@ __global__ void __launch_bounds__(kBlock)
     }
     if ((int)lane_id() == __ffs(peers) - 1 && mx != INT_MIN) atomicMax(emax + 2 * b + parity, mx);
 }
+
+template <typename T, typename IT>
+__device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64_t i,
+                                          const T2<T> *__restrict__ vel,
+                                          const T2<T> *__restrict__ prho,
+                                          const T2<T> *__restrict__ abar, const T2<T> &xi,
+                                          const T2<T> &vi, const T2<T> &ab, const T2<T> &pi,
+                                          T &gx, T &gy, T &gvx, T &gvy, T &grh, T &sumS);
+template <typename T, typename IT>
+__device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T> &xi,
+                                             const T2<T> &ab, const T2<T> &pi, T gx, T gy,
+                                             T gvx, T gvy, T grh, T sumS,
+                                             const T *__restrict__ theta,
+                                             const T *__restrict__ galpha, T2<T> *__restrict__ gXs,
+                                             T *__restrict__ grho, T2<T> *__restrict__ gV);
 
 // adj_pass1_kernel! (src/adjoint.jl:30-122) + the per-particle half of
 // adj_design_kernel! (gXs += galpha * grad alpha, src/adjoint.jl:173-175)
@@ -552,57 +697,59 @@ __global__ void __launch_bounds__(kBlock)
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     decltype(auto) I = load_inst<MULTI>(v, i);
-    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc,
-            twomumass = I.p.twomumass;
     const T2<T> xi = v.pos[i];
     const T2<T> vi = vel[i];
     const T2<T> ab = abar[i];
     const T2<T> pi = prho[i];
+    T gx, gy, gvx, gvy, grh, sumS;
+    pass1_sum<T>(v, I, i, vel, prho, abar, xi, vi, ab, pi, gx, gy, gvx, gvy, grh, sumS);
+    pass1_finish<T>(I, i, xi, ab, pi, gx, gy, gvx, gvy, grh, sumS, theta, galpha, gXs, grho, gV);
+}
+
+// The pair loop of adj_pass1_kernel! (src/adjoint.jl:41-110).
+template <typename T, typename IT>
+__device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64_t i,
+                                          const T2<T> *__restrict__ vel,
+                                          const T2<T> *__restrict__ prho,
+                                          const T2<T> *__restrict__ abar, const T2<T> &xi,
+                                          const T2<T> &vi, const T2<T> &ab, const T2<T> &pi,
+                                          T &gx, T &gy, T &gvx, T &gvy, T &grh, T &sumS)
+{
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc,
+            twomumass = I.p.twomumass;
     const T pti = pi.x, iri = pi.y;
-    T gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
+    gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
     for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < r2max) {
-            T r, rinv;
-            if constexpr (sizeof(T) == 4) {
-                rinv = r2 > (T)0 ? rsqrtf(r2) : (T)0;
-                r = r2 * rinv;
-            } else {
-                r = sqrt(r2);
-            }
-            const T q = r * invh;
-            const T u = (T)1 - (T)0.5 * q;
-            const T F = Fc * u * u * u;
-            const T G = Gc * u * u;
-            const T2<T> pj = prho[j];
-            const T Pij = m * (pti + pj.x);
-            const T Cbase = twomumass * iri * pj.y;
-            const T C = Cbase * F;
-            const T2<T> abj = abar[j];
-            const T2<T> vj = vel[j];
-            const T dax = ab.x - abj.x;
-            const T day = ab.y - abj.y;
-            const T dvx = vi.x - vj.x;
-            const T dvy = vi.y - vj.y;
-            const T ad_d = -(dax * dx + day * dy);
-            const T ad_v = dax * dvx + day * dvy;
-            gx -= Pij * F * dax;
-            gy -= Pij * F * day;
-            const T Fbar = Pij * ad_d + Cbase * ad_v;
-            T w;
-            if constexpr (sizeof(T) == 4) w = Fbar * G * invh * rinv;
-            else w = Fbar * G * invh / r;
-            gx += w * dx;
-            gy += w * dy;
-            gvx += C * dax;
-            gvy += C * day;
-            grh -= C * ad_v * iri;
-            sumS += F * ad_d;
+            const Pass1Pair<T> t = pass1_pair<T>(r2, dx, dy, invh, m, Fc, Gc, twomumass, pti, iri,
+                                                 vi, ab, prho[j], abar[j], vel[j]);
+            gx -= t.gxs;
+            gy -= t.gys;
+            gx += t.gxa;
+            gy += t.gya;
+            gvx += t.gvx;
+            gvy += t.gvy;
+            grh -= t.grs;
+            sumS += t.sS;
         }
     });
+}
+
+// Per-particle tail of adj_pass1_kernel! (src/adjoint.jl:112-121), the gXs
+// half of adj_design_kernel! and _axpy2!(gV, gVs).
+template <typename T, typename IT>
+__device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T> &xi,
+                                             const T2<T> &ab, const T2<T> &pi, T gx, T gy,
+                                             T gvx, T gvy, T grh, T sumS,
+                                             const T *__restrict__ theta,
+                                             const T *__restrict__ galpha, T2<T> *__restrict__ gXs,
+                                             T *__restrict__ grho, T2<T> *__restrict__ gV)
+{
+    const T pti = pi.x, iri = pi.y;
     const Phys<T> &p = I.p;
     grh += ((T)(-2) * p.m * pti * iri) * sumS;
     grh += p.c2 * p.m * iri * iri * sumS;
@@ -644,6 +791,14 @@ __device__ __forceinline__ void fixed_add(unsigned long long *acc, double c, int
 // 2^emax and at most n of them reach one node, so sums stay below 2^124.
 __host__ __device__ __forceinline__ int theta_scale(int emax, int lgN) { return 124 - emax - lgN; }
 
+template <typename T, typename IT>
+__device__ __forceinline__ void pass2_finish(const IT &I, int b, int64_t i, const T2<T> &xi,
+                                             T gx, T gy, const T2<T> *__restrict__ gXs,
+                                             T2<T> *__restrict__ gX,
+                                             const T *__restrict__ galpha,
+                                             const int *__restrict__ emax, int parity,
+                                             unsigned long long *__restrict__ thetaAcc);
+
 // adj_pass2_kernel! (src/adjoint.jl:126-156) + _axpy2!(gX, gXs) + the theta
 // write-back of adj_design_kernel! (src/adjoint.jl:177-184), done as an exact
 // deterministic reduction keyed by design node instead of float atomics.
@@ -669,13 +824,24 @@ __global__ void __launch_bounds__(kBlock)
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < r2max) {
-            const T q = pair_sqrt(r2) * invh;
-            const T u = (T)1 - (T)0.5 * q;
-            const T w = m * (Fc * u * u * u) * (gri + grho[j]);
+            const T w = pass2_weight<T>(r2, invh, m, Fc, gri, grho[j]);
             gx += w * dx;
             gy += w * dy;
         }
     });
+    pass2_finish<T>(I, b, i, xi, gx, gy, gXs, gX, galpha, emax, parity, thetaAcc);
+}
+
+// _axpy2!(gX, gXs) and the exact theta write-back of one particle after its
+// pass-2 pair sum (gx, gy).
+template <typename T, typename IT>
+__device__ __forceinline__ void pass2_finish(const IT &I, int b, int64_t i, const T2<T> &xi,
+                                             T gx, T gy, const T2<T> *__restrict__ gXs,
+                                             T2<T> *__restrict__ gX,
+                                             const T *__restrict__ galpha,
+                                             const int *__restrict__ emax, int parity,
+                                             unsigned long long *__restrict__ thetaAcc)
+{
     T2<T> gs = gXs[i];
     gs.x += gx;
     gs.y += gy;
