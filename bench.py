@@ -454,19 +454,50 @@ def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64, interval=4)
             "seconds": t}
 
 
+MODELS = {
+    # the reference's physics: linear EOS, Morris viscosity (parity pinned)
+    "reference": {},
+    # the physics the benchmark configurations name (Tait EOS gamma = 7,
+    # artificial viscosity alpha = 0.02); no counterpart in the reference
+    "tait-av": dict(eos=1, gamma=7, visc=1, alpha=0.02),
+}
+
+
+def select_workload(args):
+    """(params, X0, V0, theta, config, interval) of --workload and --model;
+    small and dense fix their own steps, snapshots and precision."""
+    interval = 4
+    if args.workload == "small":
+        p_d, X0, V0, theta, cfg = small_workload()
+        args.dtype, args.nsteps, args.snapshots = "f64", 5333, 0
+    elif args.workload == "dense":
+        p_d, X0, V0, theta, cfg = dense_workload()
+        args.nsteps, args.snapshots, interval = 200, 16, 1
+    else:
+        p_d, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
+                                           args.dtype)
+    p_d = dict(p_d, **MODELS[args.model])
+    cfg = dict(cfg, model=args.model)
+    if args.model != "reference":
+        cfg["workload"] += ", Tait EOS (gamma 7) + artificial viscosity (alpha 0.02)"
+    return p_d, X0, V0, theta, cfg, interval
+
+
 def run_reference(args):
     ws, rank, _ = dist_info()
-    p, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
-                                     args.dtype)
+    p, X0, V0, theta, cfg, interval = select_workload(args)
     if rank != 0:
         return
     budget = args.ref_step_seconds
     for _ in range(args.warmup):
-        cpu_sample(p, X0, V0, theta, args.dtype, budget_s=budget / 4, max_steps=2)
+        cpu_sample(p, X0, V0, theta, args.dtype, budget_s=budget / 4, max_steps=2,
+                   interval=interval)
     tot_ps, tot_t = 0.0, 0.0
     last = None
     for _ in range(args.steps):
-        last = cpu_sample(p, X0, V0, theta, args.dtype, budget_s=budget)
+        last = cpu_sample(p, X0, V0, theta, args.dtype, budget_s=budget,
+                          max_steps=args.nsteps if args.workload == "small" else 64,
+                          interval=interval)
         tot_ps += last["value"] * last["seconds"]
         tot_t += last["seconds"]
     v = tot_ps / tot_t
@@ -498,16 +529,7 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
 
-    interval = 4
-    if args.workload == "small":
-        p_d, X0, V0, theta, cfg = small_workload()
-        args.dtype, args.nsteps, args.snapshots = "f64", 5333, 0
-    elif args.workload == "dense":
-        p_d, X0, V0, theta, cfg = dense_workload()
-        args.nsteps, args.snapshots, interval = 200, 16, 1
-    else:
-        p_d, X0, V0, theta, cfg = workload(args.side, args.nsteps, args.snapshots, args.ntheta,
-                                           args.dtype)
+    p_d, X0, V0, theta, cfg, interval = select_workload(args)
     p = S.SPHParams(**p_d, dtype=args.dtype)
     N = X0.shape[1]
     pc = p.c_struct()
@@ -537,6 +559,15 @@ def run_ours(args):
     for _ in range(args.warmup):
         solve()
     torch.cuda.synchronize()
+    graph = None
+    if args.graph:
+        # the whole solve recorded once as a CUDA graph and replayed per step
+        graph = S.capture(solve)
+        for _ in range(2):
+            graph.launch()
+        torch.cuda.synchronize()
+        args.kernel_events = 0  # replays carry no per-launch events
+    run_step = graph.launch if graph is not None else solve
 
     kid = LB.KERNEL_ID[args.kernel]
     LB.check(L.sph_profile_reset())
@@ -551,12 +582,14 @@ def run_ours(args):
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        solve()
+        run_step()
     e1.record(stream)
     torch.cuda.synchronize()
     launches = L.sph_launch_count() - n0
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+    if graph is not None:
+        LB.check(L.sph_workspace_objective_value(ws.h, C.byref(J)))
     kms, kn = C.c_double(), C.c_int64()
     LB.check(L.sph_profile_read(kid, C.byref(kms), C.byref(kn)))
     LB.check(L.sph_profile_enable(kid, 0))
@@ -659,7 +692,8 @@ def run_ours(args):
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "recomputed_forward_steps_per_solve": rec,
                 "objective_J": J.value, "kernels_one_solve": kernels,
-                "block_sizes": blocks}
+                "block_sizes": blocks, "graph": graph is not None,
+                "graph_kernels_per_solve": graph.nodes if graph is not None else None}
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
@@ -678,6 +712,9 @@ def main():
     ap.add_argument("--workers", type=int, default=6, help="served: concurrent requests")
     ap.add_argument("--hbm-budget-gb", type=float, default=96.0, help="served: admission budget")
     ap.add_argument("--instances", type=int, default=64, help="batched: number of instances")
+    ap.add_argument("--model", default="reference", choices=sorted(MODELS),
+                    help="physics: the reference's (linear EOS, Morris viscosity) or Tait + "
+                         "artificial viscosity")
     ap.add_argument("--side", type=int, default=1024, help="lattice side (particles = side^2)")
     ap.add_argument("--nsteps", type=int, default=1000)
     ap.add_argument("--snapshots", type=int, default=32)
@@ -695,6 +732,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--breakdown", type=int, default=1)
+    ap.add_argument("--graph", type=int, default=0,
+                    help="time replays of the whole solve captured as one CUDA graph")
     ap.add_argument("--autotune", type=int, default=1,
                     help="measure per-kernel block sizes on the workload before timing")
     args = ap.parse_args()

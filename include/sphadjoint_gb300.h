@@ -30,10 +30,21 @@ extern "C" {
 
 #define SPH_API __attribute__((visibility("default")))
 
-/* SPHParams{T} (src/params.jl:58-72). gx/gy default to 0 / -9.81 there. */
+/* SPHParams{T} (src/params.jl:58-72). gx/gy default to 0 / -9.81 there.
+   The trailing fields select model variants that have no counterpart in the
+   reference (which has the linear EOS and Morris viscosity, README.md:505-519);
+   all zero = the reference's model:
+     eos   0 linear p = c^2 (rho - rho0); 1 Tait p = B ((rho/rho0)^gamma - 1),
+           B = c^2 rho0 / gamma, integer gamma in [1, 15] (the bracket evaluated
+           as s_{k+1} = s_k (1 + d) + d, s_1 = d = (rho - rho0)/rho0)
+     visc  0 Morris (mu); 1 Monaghan artificial viscosity, a_i += K d with
+           K = m alpha c h s F / ((r^2 + 0.01 h^2) (rho_i + rho_j) / 2) on
+           approaching pairs (s = (v_i - v_j).d < 0), alpha >= 0 */
 typedef struct sph_params {
     double h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
     int32_t ngx, ngy;
+    int32_t eos, gamma, visc, pad;
+    double alpha;
 } sph_params;
 
 typedef struct sph_state_s *sph_state;         /* State          (src/driver.jl:5-36)   */
@@ -278,6 +289,33 @@ SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_
    always use one thread per particle. Other values: SPH_ERR_ARG. */
 SPH_API int32_t sph_set_group_lanes(int32_t lanes);
 SPH_API int32_t sph_get_group_lanes(int32_t *lanes);
+
+/* ---- captured sequences (no counterpart in the reference) ----
+   sph_capture_begin records every call the calling thread makes on its library
+   stream into a CUDA graph instead of running it; sph_capture_end instantiates
+   the graph and sph_graph_launch replays it (enqueued, not waited for). While
+   capturing, calls return no host results (J, flags: 0) and never wait; read
+   them after a replay with sph_workspace_objective_value,
+   sph_state_take_flags and sph_workspace_take_flags, and the state and
+   gradients with the usual getters. Calls that would allocate device memory
+   (the first use of a state, tape, snapshot or workspace) or copy host arrays
+   (host seeds) fail while capturing: run the sequence once, then capture it.
+   A graph replays only the device work; the handles' host bookkeeping
+   (neighbour-list age, tape length, snapshot slots) stays as the capture left
+   it, so capture a sequence that starts from a reset -- for instance one whole
+   solve: sph_state_assign from a pristine state, sph_tape_reset, sph_simulate,
+   sph_objective, sph_backward_seeded -- and replay it as a unit. */
+typedef struct sph_graph_s *sph_graph;
+SPH_API int32_t sph_capture_begin(void);
+SPH_API int32_t sph_capture_end(sph_graph *out);
+SPH_API int32_t sph_graph_launch(sph_graph g);
+/* kernel launches one replay performs */
+SPH_API int32_t sph_graph_nodes(sph_graph g, int64_t *nodes);
+SPH_API int32_t sph_graph_destroy(sph_graph g);
+/* J of the last sph_objective / sph_batch_objective (one per instance), read
+   from the device; neighbour-list flags of the last backward's reverse sweep */
+SPH_API int32_t sph_workspace_objective_value(sph_workspace ws, double *J);
+SPH_API int32_t sph_workspace_take_flags(sph_workspace ws, uint32_t *flags);
 
 /* ---- instrumentation ---- */
 /* kernels launched by this library since load */

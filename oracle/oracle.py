@@ -26,7 +26,9 @@ _lib = None
 class OrcParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in
                 ("h", "m", "rho0", "c", "mu", "gx", "gy", "dt", "Lx", "Ly", "kw")] + \
-               [("ngx", C.c_int32), ("ngy", C.c_int32)]
+               [("ngx", C.c_int32), ("ngy", C.c_int32), ("eos", C.c_int32),
+                ("gamma", C.c_int32), ("visc", C.c_int32), ("pad", C.c_int32),
+                ("alpha", C.c_double)]
 
 
 def build(force: bool = False) -> str:
@@ -119,10 +121,13 @@ def get_threads() -> int:
 
 
 def params(**kw) -> OrcParams:
-    """SPHParams with the reference's defaults gx = 0, gy = -9.81."""
+    """SPHParams with the reference's defaults gx = 0, gy = -9.81 (linear EOS,
+    Morris viscosity). eos=1 selects Tait (gamma, default 7), visc=1 the
+    artificial viscosity (alpha)."""
     p = OrcParams()
     p.gx = kw.pop("gx", 0.0)
     p.gy = kw.pop("gy", -9.81)
+    p.gamma = kw.pop("gamma", 7)
     for k, v in kw.items():
         setattr(p, k, v)
     return p
@@ -271,9 +276,10 @@ def _inner_params(o, p):
     class _OP(C.Structure):
         _fields_ = [(n, R) for n in
                     ("h", "m", "rho0", "c", "mu", "gx", "gy", "dt", "Lx", "Ly", "kw")] + \
-                   [("ngx", C.c_int), ("ngy", C.c_int)]
+                   [("ngx", C.c_int), ("ngy", C.c_int), ("eos", C.c_int), ("gamma", C.c_int),
+                    ("visc", C.c_int), ("alpha", R)]
     q = _OP()
-    for n, _ in OrcParams._fields_:
+    for n, _ in _OP._fields_:
         setattr(q, n, getattr(p, n))
     return q
 

@@ -21,10 +21,16 @@
 #define M_PI 3.14159265358979323846
 #endif
 
-/* SPHParams as the caller passes it (every field double; converted to T) */
+/* SPHParams as the caller passes it (every field double; converted to T),
+   plus the equation of state and viscosity model: eos 0 = linear
+   (the reference), 1 = Tait with integer exponent gamma; visc 0 = Morris
+   (the reference), 1 = Monaghan artificial viscosity with coefficient alpha.
+   The two variants have no counterpart in the reference. */
 typedef struct {
     double h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
     int32_t ngx, ngy;
+    int32_t eos, gamma, visc, pad;
+    double alpha;
 } orc_params;
 
 void orc_set_threads(int n)

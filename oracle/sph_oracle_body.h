@@ -27,6 +27,8 @@
 typedef struct {
     R h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
     int ngx, ngy;
+    int eos, gamma, visc;
+    R alpha;
 } FN(OP);
 
 typedef struct {
@@ -65,7 +67,30 @@ static FN(OP) FN(to_params)(const orc_params *pp)
     p.mu = (R)pp->mu; p.gx = (R)pp->gx; p.gy = (R)pp->gy; p.dt = (R)pp->dt;
     p.Lx = (R)pp->Lx; p.Ly = (R)pp->Ly; p.kw = (R)pp->kw;
     p.ngx = pp->ngx; p.ngy = pp->ngy;
+    p.eos = pp->eos; p.gamma = pp->gamma; p.visc = pp->visc; p.alpha = (R)pp->alpha;
     return p;
+}
+
+/* ---- model variants (no counterpart in the reference) --------------------
+   Tait: p = B ((rho/rho0)^gamma - 1), B = c^2 rho0 / gamma. With
+   delta = (rho - rho0) / rho0 the bracket is s_gamma of s_1 = delta,
+   s_{k+1} = s_k (1 + delta) + delta (no cancellation near rho0);
+   dp/drho = (B gamma / rho0) (rho/rho0)^(gamma-1), the power a left fold.
+   Monaghan viscosity on a pair with s = (v_i - v_j).d < 0:
+   a_i += K d, K = m alpha c h s F / ((r^2 + 0.01 h^2) (rho_i + rho_j)/2). */
+static inline R FN(pow_fold)(R x, int k)
+{
+    R y = (R)1;
+    for (int t = 0; t < k; ++t) y = y * x;
+    return y;
+}
+
+static inline R FN(pow1m)(R delta, int k)
+{
+    R s = delta;
+    const R x = (R)1 + delta;
+    for (int t = 1; t < k; ++t) s = s * x + delta;
+    return s;
 }
 
 /* ---- src/kernels.jl:15-44 ------------------------------------------------- */
@@ -331,12 +356,16 @@ void FN(orc_eos)(FN(OState) *st, const FN(OP) *p)
 {
     const R c2 = p->c * p->c;
     const R rho0 = p->rho0;
+    const R B = c2 * rho0 / (R)p->gamma;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < st->N; ++i) {
         R ri = st->rho[i];
         R inv = (R)1 / ri;
         st->invrho[i] = inv;
-        st->pterm[i] = c2 * (ri - rho0) * inv * inv;
+        if (p->eos == 1)
+            st->pterm[i] = B * FN(pow1m)((ri - rho0) / rho0, p->gamma) * inv * inv;
+        else
+            st->pterm[i] = c2 * (ri - rho0) * inv * inv;
     }
 }
 
@@ -352,6 +381,8 @@ void FN(orc_accel)(FN(OState) *st, const R *theta, const FN(OP) *p, int explicit
     const R r2max = (R)4 * h * h;
     const R Fc = (R)(-5) * A * invh * invh;
     const R twomumass = (R)2 * mass * p->mu;
+    const R avc = mass * p->alpha * p->c * h;
+    const R eh2 = (R)0.01 * h * h;
     const int mx = st->maxnb;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < N; ++i) {
@@ -359,6 +390,7 @@ void FN(orc_accel)(FN(OState) *st, const R *theta, const FN(OP) *p, int explicit
         R vxi = st->V[2 * i], vyi = st->V[2 * i + 1];
         R pti = st->pterm[i];
         R iri = st->invrho[i];
+        R rhoi = st->rho[i];
         R ax = (R)0, ay = (R)0;
         const int32_t *row = st->indices + i * (int64_t)mx;
         for (int32_t m = 0; m < st->nbcount[i]; ++m) {
@@ -373,9 +405,23 @@ void FN(orc_accel)(FN(OState) *st, const R *theta, const FN(OP) *p, int explicit
                 R Pij = mass * (pti + st->pterm[j]);
                 ax -= Pij * F * dx;
                 ay -= Pij * F * dy;
-                R C = twomumass * iri * st->invrho[j] * F;
-                ax += C * (vxi - st->V[2 * j]);
-                ay += C * (vyi - st->V[2 * j + 1]);
+                if (p->visc == 1) {
+                    R wx = vxi - st->V[2 * j];
+                    R wy = vyi - st->V[2 * j + 1];
+                    R s = wx * dx + wy * dy;
+                    R K = (R)0;
+                    if (s < (R)0) {
+                        R D = r2 + eh2;
+                        R rb = (rhoi + st->rho[j]) * (R)0.5;
+                        K = avc * s * F / (D * rb);
+                    }
+                    ax += K * dx;
+                    ay += K * dy;
+                } else {
+                    R C = twomumass * iri * st->invrho[j] * F;
+                    ax += C * (vxi - st->V[2 * j]);
+                    ay += C * (vyi - st->V[2 * j + 1]);
+                }
             }
         }
         R al, d1, d2;
@@ -550,6 +596,9 @@ static void FN(adj_pass1)(FN(OWork) *ws, const FN(OState) *st, const R *theta,
     const R Fc = (R)(-5) * A * invh * invh;
     const R Gc = (R)7.5 * A * invh * invh;
     const R twomumass = (R)2 * mass * p->mu;
+    const R avc = mass * p->alpha * p->c * h;
+    const R eh2 = (R)0.01 * h * h;
+    const R dB = c2 * p->rho0 / (R)p->gamma * (R)p->gamma / p->rho0;
     const int mx = st->maxnb;
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < N; ++i) {
@@ -558,6 +607,7 @@ static void FN(adj_pass1)(FN(OWork) *ws, const FN(OState) *st, const R *theta,
         R abx = ws->abar[2 * i], aby = ws->abar[2 * i + 1];
         R pti = st->pterm[i];
         R iri = st->invrho[i];
+        R rhoi = st->rho[i];
         R gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
         const int32_t *row = st->indices + i * (int64_t)mx;
         for (int32_t m = 0; m < st->nbcount[i]; ++m) {
@@ -582,18 +632,50 @@ static void FN(adj_pass1)(FN(OWork) *ws, const FN(OState) *st, const R *theta,
                 R ad_v = dax * dvx + day * dvy;
                 gx -= Pij * F * dax;
                 gy -= Pij * F * day;
-                R Fbar = Pij * ad_d + Cbase * ad_v;
-                R w = Fbar * G * invh / r;
-                gx += w * dx;
-                gy += w * dy;
-                gvx += C * dax;
-                gvy += C * day;
-                grh -= C * ad_v * iri;
-                sumS += F * ad_d;
+                if (p->visc == 1) {
+                    /* d/d(d, v, rho) of (abar_i - abar_j).(K d) */
+                    R s = dvx * dx + dvy * dy;
+                    R Fbar = Pij * ad_d;
+                    R w = Fbar * G * invh / r;
+                    R Ad = dax * dx + day * dy;
+                    R avx = (R)0, avy = (R)0, vx = (R)0, vy = (R)0, rs = (R)0;
+                    if (s < (R)0) {
+                        R D = r2 + eh2;
+                        R rb = (rhoi + st->rho[j]) * (R)0.5;
+                        R Drb = D * rb;
+                        R K = avc * s * F / Drb;
+                        R Ks = avc * F / Drb;
+                        R KF = avc * s / Drb;
+                        R cd = Ad * (KF * G * invh / r - (R)2 * K / D);
+                        avx = K * dax + Ad * Ks * dvx + cd * dx;
+                        avy = K * day + Ad * Ks * dvy + cd * dy;
+                        vx = Ad * Ks * dx;
+                        vy = Ad * Ks * dy;
+                        rs = Ad * K / ((R)2 * rb);
+                    }
+                    gx += w * dx + avx;
+                    gy += w * dy + avy;
+                    gvx += vx;
+                    gvy += vy;
+                    grh -= rs;
+                    sumS += F * ad_d;
+                } else {
+                    R Fbar = Pij * ad_d + Cbase * ad_v;
+                    R w = Fbar * G * invh / r;
+                    gx += w * dx;
+                    gy += w * dy;
+                    gvx += C * dax;
+                    gvy += C * day;
+                    grh -= C * ad_v * iri;
+                    sumS += F * ad_d;
+                }
             }
         }
         grh += ((R)(-2) * mass * pti * iri) * sumS;
-        grh += c2 * mass * iri * iri * sumS;
+        if (p->eos == 1)
+            grh += dB * FN(pow_fold)(rhoi / p->rho0, p->gamma - 1) * mass * iri * iri * sumS;
+        else
+            grh += c2 * mass * iri * iri * sumS;
         if (explicit_drag) {
             /* tools/verify_gather.py:87-90 */
             R al = st->alpha[i];

@@ -13,6 +13,9 @@ from .api import (  # noqa: F401
     State,
     Tape,
     backward,
+    backward_seeded,
+    capture,
+    Graph,
     build,
     build_neighbors,
     group_lanes,

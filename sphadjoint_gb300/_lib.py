@@ -24,7 +24,9 @@ KERNEL_ID = {k: i for i, k in enumerate(KERNELS)}
 class sph_params(C.Structure):
     _fields_ = [(n, C.c_double) for n in
                 ("h", "m", "rho0", "c", "mu", "gx", "gy", "dt", "Lx", "Ly", "kw")] + \
-               [("ngx", C.c_int32), ("ngy", C.c_int32)]
+               [("ngx", C.c_int32), ("ngy", C.c_int32), ("eos", C.c_int32),
+                ("gamma", C.c_int32), ("visc", C.c_int32), ("pad", C.c_int32),
+                ("alpha", C.c_double)]
 
 
 class SPHError(RuntimeError):
@@ -96,6 +98,13 @@ _SIGS = {
     "sph_state_assign": (_I32, [_P, _P]),
     "sph_autotune": (_I32, [_P, _P, _I32, _I32P]),
     "sph_set_group_lanes": (_I32, [_I32]),
+    "sph_capture_begin": (_I32, []),
+    "sph_capture_end": (_I32, [_PP]),
+    "sph_graph_launch": (_I32, [_P]),
+    "sph_graph_nodes": (_I32, [_P, _I64P]),
+    "sph_graph_destroy": (_I32, [_P]),
+    "sph_workspace_objective_value": (_I32, [_P, _DP]),
+    "sph_workspace_take_flags": (_I32, [_P, _U32P]),
     "sph_get_group_lanes": (_I32, [_I32P]),
     "sph_objective": (_I32, [_P, _P, _I32, _DP, _SP, _DP]),
     "sph_backward_seeded": (_I32, [_P, _P, _P, _SP, _P, C.c_double, _I32, _I32, _U32P]),

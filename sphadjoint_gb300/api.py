@@ -22,7 +22,12 @@ _DT = {"f64": (L.SPH_F64, np.float64), "f32": (L.SPH_F32, np.float32)}
 
 @dataclass
 class SPHParams:
-    """SPHParams{T} (src/params.jl:58-72); ``dtype`` is T ("f64" or "f32")."""
+    """SPHParams{T} (src/params.jl:58-72); ``dtype`` is T ("f64" or "f32").
+
+    ``eos`` and ``visc`` select model variants that the reference does not
+    have (it uses the linear EOS and Morris viscosity): ``eos="tait"`` with
+    integer exponent ``gamma``, ``visc="artificial"`` (Monaghan) with
+    coefficient ``alpha``; ``mu`` is then unused."""
 
     h: float
     m: float
@@ -38,12 +43,25 @@ class SPHParams:
     gx: float = 0.0
     gy: float = -9.81
     dtype: str = "f64"
+    eos: str = "linear"
+    gamma: int = 7
+    visc: str = "morris"
+    alpha: float = 0.0
+
+    _EOS = {"linear": 0, "tait": 1}
+    _VISC = {"morris": 0, "artificial": 1}
 
     def c_struct(self) -> L.sph_params:
         p = L.sph_params()
         for k in ("h", "m", "rho0", "c", "mu", "gx", "gy", "dt", "Lx", "Ly", "kw"):
             setattr(p, k, float(getattr(self, k)))
         p.ngx, p.ngy = int(self.ngx), int(self.ngy)
+        try:
+            p.eos = self._EOS[self.eos] if isinstance(self.eos, str) else int(self.eos)
+            p.visc = self._VISC[self.visc] if isinstance(self.visc, str) else int(self.visc)
+        except KeyError as e:
+            raise L.ArgumentError(1, f"unknown model variant {e}") from None
+        p.gamma, p.alpha = int(self.gamma), float(self.alpha)
         return p
 
     @property
@@ -192,6 +210,12 @@ class State:
         L.check(self._L.sph_state_take_flags(self.h, C.byref(f)))
         return f.value
 
+    def assign(self, src: "State") -> "State":
+        """Make this state a device copy of src (same configuration): particles,
+        order, neighbour structure and the neighbour-list age."""
+        L.check(self._L.sph_state_assign(self.h, src.h))
+        return self
+
 
 def _warn_flags(f: int, maxnb: int):
     # check_neighbor_flags (src/neighbors.jl:282-290)
@@ -277,6 +301,30 @@ class AdjointWorkspace:
         gt = np.empty((self.p.ngx, self.p.ngy), self.p.np)  # column-major (ngy, ngx)
         L.check(self._L.sph_workspace_get(self.h, _ptr(gX), _ptr(gV), _ptr(gt)))
         return gX.T, gV.T, gt.T
+
+    def objective(self, st: "State", kind="ke_right", args=None, p: SPHParams | None = None):
+        """J of the state's current positions/velocities on the device; the
+        terminal seeds stay on the device for backward_seeded. kind:
+        "ke_right" (kinetic energy of the right half) or "target"
+        (target_objective with args = (xc, yc, sigma)). While capturing, the
+        returned J is 0: read it after a replay with objective_value()."""
+        kinds = {"ke_right": 0, "target": 1}
+        a = (C.c_double * 3)(*args) if args is not None else None
+        J = C.c_double()
+        pc = (p or self.p).c_struct()
+        L.check(self._L.sph_objective(self.h, st.h, kinds[kind], a, C.byref(pc), C.byref(J)))
+        return J.value
+
+    def objective_value(self) -> float:
+        J = C.c_double()
+        L.check(self._L.sph_workspace_objective_value(self.h, C.byref(J)))
+        return J.value
+
+    def take_flags(self) -> int:
+        """Neighbour-list flags of the last backward's reverse sweep."""
+        f = C.c_uint32()
+        L.check(self._L.sph_workspace_take_flags(self.h, C.byref(f)))
+        return f.value
 
     @property
     def gX(self):
@@ -429,6 +477,64 @@ def batch_backward(ws: BatchWorkspace, tape: Tape, theta: BatchField, seedsX=Non
     ws.last_flags = f.value
     _warn_flags(f.value, maxnb)
     return ws
+
+
+def backward_seeded(ws: AdjointWorkspace, tape: Tape, theta, p: SPHParams, scratch=None,
+                    skin=0.2, interval=4, maxnb=64) -> AdjointWorkspace:
+    """backward! seeded by the workspace's last on-device objective."""
+    th = _field(theta, p)
+    f = C.c_uint32()
+    L.check(ws._L.sph_backward_seeded(ws.h, tape.h, th.h, C.byref(p.c_struct()),
+                                      scratch.h if scratch is not None else None, float(skin),
+                                      int(interval), int(maxnb), C.byref(f)))
+    ws.last_flags = f.value
+    _warn_flags(f.value, maxnb)
+    return ws
+
+
+class Graph:
+    """A captured sequence of library calls (a CUDA graph, no counterpart in
+    the reference). launch() replays its device work on the calling thread's
+    library stream without waiting."""
+
+    def __init__(self, h):
+        self._L = L.load()
+        self.h = h
+
+    def launch(self) -> "Graph":
+        L.check(self._L.sph_graph_launch(self.h))
+        return self
+
+    @property
+    def nodes(self) -> int:
+        n = C.c_int64()
+        L.check(self._L.sph_graph_nodes(self.h, C.byref(n)))
+        return n.value
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_graph_destroy(self.h)
+            self.h = None
+
+
+def capture(fn) -> Graph:
+    """Record the library calls fn() makes on this thread into a Graph instead
+    of running them. Run the same sequence once before capturing it (first uses
+    allocate); host results (J, flags) read as 0 during capture."""
+    lib = L.load()
+    L.check(lib.sph_capture_begin())
+    g = C.c_void_p()
+    try:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            fn()
+    except BaseException:
+        lib.sph_capture_end(C.byref(g))
+        if g.value:
+            lib.sph_graph_destroy(g)
+        raise
+    L.check(lib.sph_capture_end(C.byref(g)))
+    return Graph(g)
 
 
 def reset(tape: Tape) -> Tape:

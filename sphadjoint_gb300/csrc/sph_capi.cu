@@ -24,6 +24,7 @@ thread_local cudaStream_t g_stream = nullptr;
 thread_local bool g_stream_external = false;
 std::atomic<long long> g_launches{0};
 std::atomic<int> g_group_lanes{0};
+thread_local bool g_capturing = false;
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {};
 
@@ -100,20 +101,27 @@ static cudaEvent_t timer_event(KTimer &t)
 void rt_before_launch(int kid)
 {
     KTimer &t = g_timer[kid];
-    if (t.on) cuda_check(cudaEventRecord(timer_event(t), rt_stream()), "cudaEventRecord");
+    if (t.on && !g_capturing) cuda_check(cudaEventRecord(timer_event(t), rt_stream()), "cudaEventRecord");
 }
 
 void rt_after_launch(int kid)
 {
     g_launches.fetch_add(1, std::memory_order_relaxed);
     KTimer &t = g_timer[kid];
-    if (t.on) {
+    if (t.on && !g_capturing) {
         cuda_check(cudaEventRecord(timer_event(t), rt_stream()), "cudaEventRecord");
         t.launches += 1;
     }
 }
 
 void rt_check_launch(const char *name) { cuda_check(cudaGetLastError(), name); }
+
+bool rt_capturing() { return g_capturing; }
+
+void rt_sync()
+{
+    if (!g_capturing) cuda_check(cudaStreamSynchronize(rt_stream()), "cudaStreamSynchronize");
+}
 
 int rt_group_lanes() { return g_group_lanes.load(std::memory_order_relaxed); }
 void rt_set_group_lanes(int lanes) { g_group_lanes.store(lanes, std::memory_order_relaxed); }
@@ -215,6 +223,7 @@ static Params to_params(const sph_params *p)
     q.h = p->h; q.m = p->m; q.rho0 = p->rho0; q.c = p->c; q.mu = p->mu; q.gx = p->gx;
     q.gy = p->gy; q.dt = p->dt; q.Lx = p->Lx; q.Ly = p->Ly; q.kw = p->kw;
     q.ngx = p->ngx; q.ngy = p->ngy;
+    q.eos = p->eos; q.gamma = p->gamma; q.visc = p->visc; q.alpha = p->alpha;
     return q;
 }
 
@@ -381,7 +390,7 @@ SPH_API int32_t sph_simulate(sph_state st, sph_field theta, const sph_params *p,
         Params q;
         if (p) q = to_params(p);
         ST(st)->simulate(FD(theta), p ? &q : nullptr, nsteps, tape ? TP(tape) : nullptr);
-        const uint32_t f = ST(st)->take_flags();
+        const uint32_t f = rt_capturing() ? 0u : ST(st)->take_flags();
         if (flags) *flags = f;
     });
 }
@@ -634,6 +643,108 @@ SPH_API int32_t sph_batch_objective(sph_workspace ws, sph_state st, int32_t kind
 SPH_API int32_t sph_workspace_get(sph_workspace ws, void *gX, void *gV, void *gtheta)
 {
     return guarded([&] { need(ws, "workspace"); WS(ws)->get(gX, gV, gtheta); });
+}
+
+SPH_API int32_t sph_workspace_objective_value(sph_workspace ws, double *J)
+{
+    return guarded([&] {
+        need(ws, "workspace");
+        need(J, "J");
+        WS(ws)->objective_value(J);
+    });
+}
+
+SPH_API int32_t sph_workspace_take_flags(sph_workspace ws, uint32_t *flags)
+{
+    return guarded([&] {
+        need(ws, "workspace");
+        const uint32_t f = WS(ws)->take_flags();
+        if (flags) *flags = f;
+    });
+}
+
+// ---- captured sequences (CUDA graphs) ----------------------------------------
+struct GraphH {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    int64_t nodes = 0;
+};
+
+SPH_API int32_t sph_capture_begin(void)
+{
+    return guarded([&] {
+        if (g_capturing) throw Error(ERR_STATE, "this thread is already capturing");
+        cuda_check(cudaStreamBeginCapture(rt_stream(), cudaStreamCaptureModeThreadLocal),
+                   "cudaStreamBeginCapture");
+        g_capturing = true;
+    });
+}
+
+SPH_API int32_t sph_capture_end(sph_graph *out)
+{
+    return guarded([&] {
+        if (!g_capturing) throw Error(ERR_STATE, "this thread is not capturing");
+        g_capturing = false;
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(rt_stream(), &g);
+        if (e != cudaSuccess || !g) {
+            if (g) cudaGraphDestroy(g);
+            (void)cudaGetLastError();
+            throw Error(ERR_STATE, std::string("the captured sequence is invalid: ") +
+                                       cudaGetErrorString(e));
+        }
+        need(out, "out");
+        auto *h = new GraphH();
+        h->g = g;
+        // count the kernel nodes (the launch counter adds them per replay)
+        size_t n = 0;
+        (void)cudaGraphGetNodes(g, nullptr, &n);
+        std::vector<cudaGraphNode_t> nodes(n);
+        if (n) (void)cudaGraphGetNodes(g, nodes.data(), &n);
+        for (size_t k = 0; k < n; ++k) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+                h->nodes += 1;
+        }
+        (void)cudaGetLastError();
+        const cudaError_t ei = cudaGraphInstantiate(&h->x, g, 0);
+        if (ei != cudaSuccess) {
+            cudaGraphDestroy(g);
+            delete h;
+            cuda_check(ei, "cudaGraphInstantiate");
+        }
+        *out = reinterpret_cast<sph_graph>(h);
+    });
+}
+
+SPH_API int32_t sph_graph_launch(sph_graph g)
+{
+    return guarded([&] {
+        need(g, "graph");
+        auto *h = reinterpret_cast<GraphH *>(g);
+        cuda_check(cudaGraphLaunch(h->x, rt_stream()), "cudaGraphLaunch");
+        g_launches.fetch_add(h->nodes, std::memory_order_relaxed);
+    });
+}
+
+SPH_API int32_t sph_graph_nodes(sph_graph g, int64_t *nodes)
+{
+    return guarded([&] {
+        need(g, "graph");
+        need(nodes, "nodes");
+        *nodes = reinterpret_cast<GraphH *>(g)->nodes;
+    });
+}
+
+SPH_API int32_t sph_graph_destroy(sph_graph g)
+{
+    return guarded([&] {
+        if (!g) return;
+        auto *h = reinterpret_cast<GraphH *>(g);
+        if (h->x) cudaGraphExecDestroy(h->x);
+        if (h->g) cudaGraphDestroy(h->g);
+        delete h;
+    });
 }
 
 SPH_API int64_t sph_launch_count(void) { return (int64_t)g_launches.load(); }

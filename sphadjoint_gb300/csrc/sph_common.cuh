@@ -51,7 +51,30 @@ template <typename T> struct Phys {
     int ngx, ngy;
     T A, invh, r2max, Fc, Gc, twomumass, c2;
     T hxg, hyg, ngx1, ngy1, gxmax, gymax;
+    // model variants (no counterpart in the reference): eos 1 = Tait with
+    // exponent gam, visc 1 = Monaghan artificial viscosity; B = c^2 rho0 /
+    // gam, dB = B gam / rho0, avc = m alpha c h, eh2 = 0.01 h^2
+    int eos, gam, visc;
+    T B, dB, avc, eh2;
 };
+
+// x^k as a left fold of products (the Tait derivative; same order in the oracle)
+template <typename T> __device__ __forceinline__ T pow_fold(T x, int k)
+{
+    T y = (T)1;
+    for (int t = 0; t < k; ++t) y = y * x;
+    return y;
+}
+
+// (1 + delta)^k - 1 as s_1 = delta, s_{j+1} = s_j (1 + delta) + delta: the Tait
+// bracket without the cancellation of x^k - 1 near rho0
+template <typename T> __device__ __forceinline__ T pow1m(T delta, int k)
+{
+    T s = delta;
+    const T x = (T)1 + delta;
+    for (int t = 1; t < k; ++t) s = s * x + delta;
+    return s;
+}
 
 // Per-instance constants. A State is one instance; a batch packs B instances
 // (uneven particle counts, their own parameters, cell grids and design

@@ -237,13 +237,15 @@ template <typename T, int G, int NG>
 __device__ __forceinline__ void accel_sum_coop(const Group<G> &g, T (*buf)[4][G],
                                                const NLView<T> &v, const Inst<T> &I, int64_t i,
                                                uint32_t cc, const T2<T> *__restrict__ vel,
-                                               const T2<T> *__restrict__ prho, const T2<T> &xi,
+                                               const T2<T> *__restrict__ prho,
+                                               const T *__restrict__ rho, const T2<T> &xi,
                                                const T2<T> &vi, T &ax, T &ay)
 {
-    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc,
-            twomumass = I.p.twomumass;
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc;
+    const Visc<T> vc = visc_of<T>(I);
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
+    const T rhoi = vc.kind == 1 ? rho[i] : (T)0;
     Cands<T> cd;
     cd.init(v, I, i, cc, v.tmask ? v.tmask : v.masks);
     const int K = cd.total();
@@ -261,7 +263,9 @@ __device__ __forceinline__ void accel_sum_coop(const Group<G> &g, T (*buf)[4][G]
             const T r2 = dx * dx + dy * dy;
             if (r2 < r2max) {
                 in = true;
-                t = accel_pair<T>(r2, dx, dy, invh, m, Fc, twomumass, pti, iri, vi, prho[j], vel[j]);
+                const T rhoj = vc.kind == 1 ? rho[j] : (T)0;
+                t = accel_pair<T>(r2, dx, dy, invh, m, Fc, vc, pti, iri, rhoi, rhoj, vi, prho[j],
+                                  vel[j]);
             }
         }
         buf[g.gi][0][g.gl] = t.px;
@@ -290,7 +294,8 @@ __device__ __forceinline__ void accel_sum_coop(const Group<G> &g, T (*buf)[4][G]
 template <typename T, int G>
 __global__ void __launch_bounds__(kCoopBlock)
     k_accel_integrate_coop(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
-                           const T2<T> *__restrict__ prho, const T *__restrict__ theta,
+                           const T2<T> *__restrict__ prho, const T *__restrict__ rho,
+                           const T *__restrict__ theta,
                            T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
                            T2<T> *__restrict__ aOut, T *__restrict__ alphaOut,
                            uint32_t *__restrict__ flags)
@@ -307,9 +312,9 @@ __global__ void __launch_bounds__(kCoopBlock)
     T ax, ay;
     if (cc >> 31) {
         if (g.gl != 0) return;
-        accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+        accel_sum<T, true>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
     } else {
-        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, xi, vi, ax, ay);
+        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, rho, xi, vi, ax, ay);
         if (g.gl != 0) return;
     }
     accel_integrate_finish<T>(I, 0, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags);
@@ -320,7 +325,8 @@ __global__ void __launch_bounds__(kCoopBlock)
 template <typename T, int G>
 __global__ void __launch_bounds__(kCoopBlock)
     k_accel_drag_adj_coop(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
-                          const T2<T> *__restrict__ prho, const T *__restrict__ theta,
+                          const T2<T> *__restrict__ prho, const T *__restrict__ rho,
+                          const T *__restrict__ theta,
                           const T2<T> *__restrict__ gX, T2<T> *__restrict__ gV,
                           T2<T> *__restrict__ abar, T *__restrict__ galpha,
                           int *__restrict__ emax, int parity)
@@ -337,9 +343,9 @@ __global__ void __launch_bounds__(kCoopBlock)
     T ax, ay;
     if (cc >> 31) {
         if (g.gl != 0) return;
-        accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+        accel_sum<T, true>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
     } else {
-        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, xi, vi, ax, ay);
+        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, rho, xi, vi, ax, ay);
         if (g.gl != 0) return;
     }
     const int e = drag_adj_finish<T>(I, i, xi, vi, ax, ay, theta, gX, gV, abar, galpha);
@@ -351,7 +357,8 @@ __global__ void __launch_bounds__(kCoopBlock)
 template <typename T, int G>
 __global__ void __launch_bounds__(kCoopBlock)
     k_pass1_design_coop(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
-                        const T2<T> *__restrict__ prho, const T *__restrict__ theta,
+                        const T2<T> *__restrict__ prho, const T *__restrict__ rho,
+                        const T *__restrict__ theta,
                         const T2<T> *__restrict__ abar, const T *__restrict__ galpha,
                         T2<T> *__restrict__ gXs, T *__restrict__ grho, T2<T> *__restrict__ gV)
 {
@@ -369,11 +376,13 @@ __global__ void __launch_bounds__(kCoopBlock)
     T gx, gy, gvx, gvy, grh, sumS;
     if (cc >> 31) {
         if (g.gl != 0) return;
-        pass1_sum<T>(v, I, i, vel, prho, abar, xi, vi, ab, pi, gx, gy, gvx, gvy, grh, sumS);
+        pass1_sum<T, true>(v, I, i, vel, prho, rho, abar, xi, vi, ab, pi, gx, gy, gvx, gvy, grh,
+                           sumS);
     } else {
-        const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc,
-                twomumass = I.p.twomumass;
+        const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc;
+        const Visc<T> vc = visc_of<T>(I);
         const T pti = pi.x, iri = pi.y;
+        const T rhoi = vc.kind == 1 ? rho[i] : (T)0;
         Cands<T> cd;
         cd.init(v, I, i, cc, v.tmask ? v.tmask : v.masks);
         const int K = cd.total();
@@ -402,8 +411,9 @@ __global__ void __launch_bounds__(kCoopBlock)
                 const T r2 = dx * dx + dy * dy;
                 if (r2 < r2max) {
                     in = true;
-                    t = pass1_pair<T>(r2, dx, dy, invh, m, Fc, Gc, twomumass, pti, iri, vi, ab,
-                                      prho[j], abar[j], vel[j]);
+                    const T rhoj = vc.kind == 1 ? rho[j] : (T)0;
+                    t = pass1_pair<T>(r2, dx, dy, invh, m, Fc, Gc, vc, pti, iri, rhoi, rhoj, vi,
+                                      ab, prho[j], abar[j], vel[j]);
                 }
             }
             b[0][g.gl] = t.gxs;
@@ -434,7 +444,9 @@ __global__ void __launch_bounds__(kCoopBlock)
         sumS = g.from(acc, 5);
         if (g.gl != 0) return;
     }
-    pass1_finish<T>(I, i, xi, ab, pi, gx, gy, gvx, gvy, grh, sumS, theta, galpha, gXs, grho, gV);
+    const T rhoi = needs_rho_dev(I) ? rho[i] : (T)0;
+    pass1_finish<T>(I, i, xi, ab, pi, rhoi, gx, gy, gvx, gvy, grh, sumS, theta, galpha, gXs, grho,
+                    gV);
 }
 
 // adj_pass2_kernel! + _axpy2!(gX, gXs) + the exact theta write-back.

@@ -64,6 +64,9 @@ template <typename T> struct DevBuf {
     }
     void alloc(size_t count)
     {
+        if (count && rt_capturing())
+            throw Error(ERR_STATE, "device allocation while capturing a graph: run the sequence "
+                                   "once before capturing it");
         release();
         own = true;
         n = count;
@@ -165,6 +168,16 @@ template <typename T> Phys<T> make_phys(const Params &q)
     p.hyg = p.Ly / p.ngy1;
     p.gxmax = p.ngx1 - (T)1e-6;
     p.gymax = p.ngy1 - (T)1e-6;
+    // model variants: Tait B = c^2 rho0 / gamma, dB = B gamma / rho0;
+    // artificial viscosity avc = m alpha c h, eh2 = 0.01 h^2
+    p.eos = q.eos;
+    p.gam = q.gamma;
+    p.visc = q.visc;
+    const T gam = (T)(q.eos == 1 ? q.gamma : 1);
+    p.B = p.c2 * p.rho0 / gam;
+    p.dB = p.B * gam / p.rho0;
+    p.avc = p.m * (T)q.alpha * p.c * p.h;
+    p.eh2 = (T)0.01 * p.h * p.h;
     return p;
 }
 
@@ -172,7 +185,16 @@ inline void check_params(const Params &p)
 {
     if (!(p.h > 0)) throw Error(ERR_ARG, "h must be positive");
     if (p.ngx < 2 || p.ngy < 2) throw Error(ERR_ARG, "ngx and ngy must be at least 2");
+    if (p.eos != 0 && p.eos != 1) throw Error(ERR_ARG, "eos must be 0 (linear) or 1 (Tait)");
+    if (p.eos == 1 && (p.gamma < 1 || p.gamma > 15))
+        throw Error(ERR_ARG, "Tait exponent gamma must be an integer in [1, 15]");
+    if (p.visc != 0 && p.visc != 1)
+        throw Error(ERR_ARG, "visc must be 0 (Morris) or 1 (artificial viscosity)");
+    if (p.visc == 1 && !(p.alpha >= 0)) throw Error(ERR_ARG, "alpha must be >= 0");
 }
+
+// the model reads per-particle densities (Tait derivative, viscosity average)
+inline bool needs_rho(const Params &p) { return p.eos == 1 || p.visc == 1; }
 
 // exclusive scan of n int32 -> out[0..n] (+ optional copy); tmp >= blocks
 inline void scan_excl(const int32_t *in, int64_t n, int32_t *out, int32_t *out2, int32_t *tmp)
@@ -274,6 +296,8 @@ template <typename T> class Sys final : public StateI {
     DevBuf<int32_t> clStart, clOrder; // build! without a neighbour rebuild
     bool cellsOnlyLatest = false;
     bool keepAccel = false;
+    bool anyRho = false; // some instance's model reads densities in the adjoint
+    bool anyAV = false;  // some instance uses the artificial viscosity
 
     Sys(const Params &p, int64_t N, const void *X0, const void *V0, NLOpts o)
         : Sys(std::vector<Params>{p}, std::vector<int64_t>{N}, X0, V0, o)
@@ -341,6 +365,10 @@ template <typename T> class Sys final : public StateI {
         N_ = off;
         ncell = coff;
         nnode = toff;
+        for (const Params &q : ps) {
+            anyRho = anyRho || needs_rho(q);
+            anyAV = anyAV || q.visc == 1;
+        }
         nx = hinst[0].nx;
         ny = hinst[0].ny;
         {
@@ -450,6 +478,8 @@ template <typename T> class Sys final : public StateI {
         prm = *p;
         prms[0] = *p;
         hinst[0].p = make_phys<T>(*p);
+        anyRho = needs_rho(*p);
+        anyAV = p->visc == 1;
         upload_inst();
     }
 
@@ -647,15 +677,16 @@ template <typename T> class Sys final : public StateI {
             SPH_LAUNCH_COOP(K_DENSITY, G, kd, N_, v, rho.p, prho.p, tmask.p);
             v.tmask = tmask.p;
             auto ki = G == 32 ? &k_accel_integrate_coop<T, 32> : &k_accel_integrate_coop<T, 16>;
-            SPH_LAUNCH_COOP(K_ACCEL_INTEGRATE, G, ki, N_, v, vel[cur].p, prho.p, theta,
+            SPH_LAUNCH_COOP(K_ACCEL_INTEGRATE, G, ki, N_, v, vel[cur].p, prho.p, rho.p, theta,
                             pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
         } else {
             auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
             SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rho.p, prho.p, tmask.p);
             v.tmask = tmask.p;
-            auto ki = B > 1 ? &k_accel_integrate<T, true> : &k_accel_integrate<T, false>;
-            SPH_LAUNCH_TUNED(K_ACCEL_INTEGRATE, B > 1, ki, N_, v, vel[cur].p, prho.p, theta,
-                             pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
+            auto ki = B > 1 ? (anyAV ? &k_accel_integrate<T, true, true> : &k_accel_integrate<T, true>)
+                            : (anyAV ? &k_accel_integrate<T, false, true> : &k_accel_integrate<T, false>);
+            SPH_LAUNCH_TUNED(K_ACCEL_INTEGRATE, B > 1, ki, N_, v, vel[cur].p, prho.p, rho.p,
+                             theta, pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
         }
         cur = nxt;
     }
@@ -767,8 +798,11 @@ template <typename T> class Sys final : public StateI {
             prm = o->prm;
             prms = o->prms;
             hinst = o->hinst;
+            anyRho = o->anyRho;
+            anyAV = o->anyAV;
             upload_inst();
         }
+        rho.copy_from(o->rho);
         cellsOnlyLatest = false;
     }
 
@@ -778,6 +812,8 @@ template <typename T> class Sys final : public StateI {
             prm = o.prm;
             prms = o.prms;
             hinst = o.hinst;
+            anyRho = o.anyRho;
+            anyAV = o.anyAV;
             upload_inst();
         }
     }
@@ -987,7 +1023,7 @@ void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tap
         }
         step_impl(th->th.p, tx, tv);
     }
-    SPH_CK(cudaStreamSynchronize(rt_stream()));
+    rt_sync();
     rt_check_launch("simulate");
 }
 
@@ -1015,6 +1051,8 @@ template <typename T> class Work final : public WorkI {
     DevBuf<T2<T>> devSeedX, devSeedV; // seeds written by objective()
     DevBuf<double> partial;
     std::unique_ptr<Sys<T>> own;
+    Sys<T> *lastS = nullptr; // scratch state of the last backward (its flags)
+    int64_t jOff = -1;       // J slots of the last objective in `partial`
     bool haveResult = false;
     bool haveDevSeeds = false;
 
@@ -1089,18 +1127,19 @@ template <typename T> class Work final : public WorkI {
         if (did) gcur = g2;
         NLView<T> v = S.view();
         const T2<T> *vel = S.vel[S.cur].p;
+        T *rhoOut = S.anyRho ? S.rho.p : (T *)nullptr; // densities only where the model reads them
         if (const int G = S.group_lanes()) {
             const bool g32 = G == 32;
             auto kd = g32 ? &k_density_eos_coop<T, 32> : &k_density_eos_coop<T, 16>;
             auto ka = g32 ? &k_accel_drag_adj_coop<T, 32> : &k_accel_drag_adj_coop<T, 16>;
             auto k1 = g32 ? &k_pass1_design_coop<T, 32> : &k_pass1_design_coop<T, 16>;
             auto k2 = g32 ? &k_pass2_axpy_coop<T, 32> : &k_pass2_axpy_coop<T, 16>;
-            SPH_LAUNCH_COOP(K_DENSITY, G, kd, N_, v, (T *)nullptr, S.prho.p, S.tmask.p);
+            SPH_LAUNCH_COOP(K_DENSITY, G, kd, N_, v, rhoOut, S.prho.p, S.tmask.p);
             v.tmask = S.tmask.p;
-            SPH_LAUNCH_COOP(K_ACCEL_DRAG, G, ka, N_, v, vel, S.prho.p, theta, gX[gcur].p,
+            SPH_LAUNCH_COOP(K_ACCEL_DRAG, G, ka, N_, v, vel, S.prho.p, S.rho.p, theta, gX[gcur].p,
                             gV[gcur].p, abar.p, galpha.p, emax.p, parity);
-            SPH_LAUNCH_COOP(K_PASS1, G, k1, N_, v, vel, S.prho.p, theta, abar.p, galpha.p, gXs.p,
-                            grho.p, gV[gcur].p);
+            SPH_LAUNCH_COOP(K_PASS1, G, k1, N_, v, vel, S.prho.p, S.rho.p, theta, abar.p,
+                            galpha.p, gXs.p, grho.p, gV[gcur].p);
             SPH_LAUNCH_COOP(K_PASS2, G, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p,
                             parity, thetaAcc.p);
             pendingTheta = parity;
@@ -1108,15 +1147,18 @@ template <typename T> class Work final : public WorkI {
         }
         const bool multi = S.B > 1;
         auto kd = multi ? &k_density_eos<T, true> : &k_density_eos<T, false>;
-        auto ka = multi ? &k_accel_drag_adj<T, true> : &k_accel_drag_adj<T, false>;
-        auto k1 = multi ? &k_pass1_design<T, true> : &k_pass1_design<T, false>;
+        const bool av = S.anyAV;
+        auto ka = multi ? (av ? &k_accel_drag_adj<T, true, true> : &k_accel_drag_adj<T, true>)
+                        : (av ? &k_accel_drag_adj<T, false, true> : &k_accel_drag_adj<T, false>);
+        auto k1 = multi ? (av ? &k_pass1_design<T, true, true> : &k_pass1_design<T, true>)
+                        : (av ? &k_pass1_design<T, false, true> : &k_pass1_design<T, false>);
         auto k2 = multi ? &k_pass2_axpy<T, true> : &k_pass2_axpy<T, false>;
-        SPH_LAUNCH_TUNED(K_DENSITY, multi, kd, N_, v, (T *)nullptr, S.prho.p, S.tmask.p);
+        SPH_LAUNCH_TUNED(K_DENSITY, multi, kd, N_, v, rhoOut, S.prho.p, S.tmask.p);
         v.tmask = S.tmask.p;
-        SPH_LAUNCH_TUNED(K_ACCEL_DRAG, multi, ka, N_, v, vel, S.prho.p, theta, gX[gcur].p,
+        SPH_LAUNCH_TUNED(K_ACCEL_DRAG, multi, ka, N_, v, vel, S.prho.p, S.rho.p, theta, gX[gcur].p,
                          gV[gcur].p, abar.p, galpha.p, emax.p, parity);
-        SPH_LAUNCH_TUNED(K_PASS1, multi, k1, N_, v, vel, S.prho.p, theta, abar.p, galpha.p, gXs.p,
-                         grho.p, gV[gcur].p);
+        SPH_LAUNCH_TUNED(K_PASS1, multi, k1, N_, v, vel, S.prho.p, S.rho.p, theta, abar.p,
+                         galpha.p, gXs.p, grho.p, gV[gcur].p);
         SPH_LAUNCH_TUNED(K_PASS2, multi, k2, N_, v, grho.p, gXs.p, gX[gcur].p, galpha.p, emax.p,
                          parity, thetaAcc.p);
         pendingTheta = parity;
@@ -1174,12 +1216,25 @@ template <typename T> class Work final : public WorkI {
             rt_after_launch(K_MISC);
             pofs += nb;
         }
+        jOff = nbTot;
+        haveDevSeeds = true;
+        if (rt_capturing()) return; // J stays on the device (objective_value)
         SPH_CK(cudaMemcpyAsync(Jb.data(), partial.p + nbTot, sizeof(double) * B, cudaMemcpyDeviceToHost, rt_stream()));
         SPH_CK(cudaStreamSynchronize(rt_stream()));
         for (int b = 0; b < B; ++b)
             if (J) J[b] = st->hinst[b].n ? Jb[b] : 0.0;
-        haveDevSeeds = true;
     }
+
+    void objective_value(double *J) override
+    {
+        if (jOff < 0) throw Error(ERR_STATE, "no objective has run on this workspace");
+        std::vector<double> Jb((size_t)B, 0.0);
+        SPH_CK(cudaMemcpyAsync(Jb.data(), partial.p + jOff, sizeof(double) * B, cudaMemcpyDeviceToHost, rt_stream()));
+        SPH_CK(cudaStreamSynchronize(rt_stream()));
+        for (int b = 0; b < B; ++b) J[b] = ns[b] ? Jb[b] : 0.0;
+    }
+
+    uint32_t take_flags() override { return lastS ? lastS->take_flags() : 0u; }
 
     void get(void *gXo, void *gVo, void *gth) override
     {
@@ -1254,7 +1309,7 @@ template <typename T> class Tuner {
         tuned_block<T>(K_DENSITY, multi) = b;
         v.tmask = S.tmask.p;
         b = timeit([&](int c) {
-            ki<<<grid(c), c, 0, st>>>(v, S.vel[S.cur].p, S.prho.p, th.th.p, S.pos[nxt].p,
+            ki<<<grid(c), c, 0, st>>>(v, S.vel[S.cur].p, S.prho.p, S.rho.p, th.th.p, S.pos[nxt].p,
                                       S.vel[nxt].p, nullptr, nullptr, S.flags.p);
         });
         tuned_block<T>(K_ACCEL_INTEGRATE, multi) = b;
@@ -1269,16 +1324,16 @@ template <typename T> class Tuner {
         const std::vector<int> init(2 * (size_t)S.B, INT_MIN);
         SPH_CK(cudaMemcpyAsync(w.emax.p, init.data(), sizeof(int) * init.size(), cudaMemcpyHostToDevice, st));
         const T2<T> *vel = S.vel[S.cur].p;
-        ka<<<grid(kBlock), kBlock, 0, st>>>(v, vel, S.prho.p, th.th.p, w.gX[0].p, w.gV[0].p,
-                                            w.abar.p, w.galpha.p, w.emax.p, 0);
+        ka<<<grid(kBlock), kBlock, 0, st>>>(v, vel, S.prho.p, S.rho.p, th.th.p, w.gX[0].p,
+                                            w.gV[0].p, w.abar.p, w.galpha.p, w.emax.p, 0);
         b = timeit([&](int c) {
-            ka<<<grid(c), c, 0, st>>>(v, vel, S.prho.p, th.th.p, w.gX[0].p, w.gV[1].p, w.abar.p,
-                                      w.galpha.p, w.emax.p, 1);
+            ka<<<grid(c), c, 0, st>>>(v, vel, S.prho.p, S.rho.p, th.th.p, w.gX[0].p, w.gV[1].p,
+                                      w.abar.p, w.galpha.p, w.emax.p, 1);
         });
         tuned_block<T>(K_ACCEL_DRAG, multi) = b;
         b = timeit([&](int c) {
-            k1<<<grid(c), c, 0, st>>>(v, vel, S.prho.p, th.th.p, w.abar.p, w.galpha.p, w.gXs.p,
-                                      w.grho.p, w.gV[1].p);
+            k1<<<grid(c), c, 0, st>>>(v, vel, S.prho.p, S.rho.p, th.th.p, w.abar.p, w.galpha.p,
+                                      w.gXs.p, w.grho.p, w.gV[1].p);
         });
         tuned_block<T>(K_PASS1, multi) = b;
         b = timeit([&](int c) {
@@ -1351,6 +1406,10 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     }
 
     // seeds: copyto!(gX, seedX), copyto!(gV, seedV), id order -> S's cell order
+    if (rt_capturing() && !devSeeds && (seedX || seedV))
+        throw Error(ERR_STATE, "host seeds cannot be captured: use the on-device objective and "
+                               "backward_seeded inside a captured sequence");
+    lastS = S;
     gcur = 0;
     if (N_ && devSeeds) {
         SPH_LAUNCH(K_MISC, k_gather_from_ids<T>, N_, N_, S->perm.p, devSeedX.p, gX[0].p);
@@ -1371,11 +1430,7 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     }
     gtheta.zero();
     thetaAcc.zero();
-    {
-        const std::vector<int> init(2 * (size_t)B, INT_MIN);
-        SPH_CK(cudaMemcpyAsync(emax.p, init.data(), sizeof(int) * init.size(), cudaMemcpyHostToDevice, rt_stream()));
-        SPH_CK(cudaStreamSynchronize(rt_stream()));
-    }
+    SPH_LAUNCH(K_MISC, k_fill_int, 2 * (int64_t)B, 2 * (int64_t)B, emax.p, INT_MIN);
 
     const int64_t L = tp->n_;
     pendingTheta = -1;
@@ -1461,9 +1516,10 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gX[gcur].p, outX.p);
     SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gV[gcur].p, outV.p);
     haveResult = true;
-    SPH_CK(cudaStreamSynchronize(rt_stream()));
+    rt_sync();
     rt_check_launch("backward");
-    uint32_t f = S->take_flags();
+    // while capturing, the flags stay on the device (take_flags after a replay)
+    const uint32_t f = rt_capturing() ? 0u : S->take_flags();
     if (flagsOut) *flagsOut = f;
 }
 

@@ -13,9 +13,14 @@
 namespace sphgb {
 
 // SPHParams (src/params.jl:58-72); fields are converted to T by the engine.
+// eos / gamma / visc / alpha select the model variants (no counterpart in the
+// reference): eos 0 linear, 1 Tait with integer exponent gamma; visc 0 Morris,
+// 1 Monaghan artificial viscosity with coefficient alpha.
 struct Params {
     double h, m, rho0, c, mu, gx, gy, dt, Lx, Ly, kw;
     int32_t ngx, ngy;
+    int32_t eos = 0, gamma = 7, visc = 0, pad = 0;
+    double alpha = 0.0;
 };
 
 // NeighborList knobs (src/neighbors.jl:174-175).
@@ -82,6 +87,12 @@ void rt_check_launch(const char *name);
 // 16 or 32 = groups for every single-instance state.
 int rt_group_lanes();
 void rt_set_group_lanes(int lanes);
+// True while the calling thread records its library stream into a CUDA graph:
+// host reads and synchronisations are skipped (results stay on the device)
+// and device allocations are refused.
+bool rt_capturing();
+// Wait for the library stream unless it is being captured.
+void rt_sync();
 
 class FieldI {
   public:
@@ -151,6 +162,10 @@ class WorkI {
                            double *J) = 0;
     virtual void backward_seeded(TapeI *tape, FieldI *theta, const Params *p, StateI *scratch,
                                  NLOpts opts, uint32_t *flags) = 0;
+    // J of the last objective() as the device holds it (one per instance)
+    virtual void objective_value(double *J) = 0;
+    // neighbour-list flags of the last backward's reverse sweep (read and cleared)
+    virtual uint32_t take_flags() = 0;
 };
 
 #define SPH_DECLARE_FACTORIES(SFX)                                                           \

@@ -275,6 +275,12 @@ __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restri
 // integrate_kernel! (fused; positions and velocities double-buffered because
 // neighbours read the pre-step state).
 // ---------------------------------------------------------------------------
+// The model reads per-particle densities (Tait derivative, viscosity average).
+template <typename IT> __device__ __forceinline__ bool needs_rho_dev(const IT &I)
+{
+    return I.p.eos == 1 || I.p.visc == 1;
+}
+
 // Per-pair terms, shared by the thread-per-particle kernels and the
 // group-per-particle kernels (sph_coop.cuh): each kernel adds them into its
 // running sums in slot order, so both forms round identically.
@@ -289,14 +295,33 @@ __device__ __forceinline__ T density_pair(T r2, T invh, T m, T A)
     return m * (A * u2 * u2 * ((T)2 * q + (T)1));
 }
 
-// accel_kernel!: a_i -= P F d, then a_i += C (v_i - v_j), per component.
+// Viscosity constants of one instance, hoisted out of the pair loops: kind 0
+// Morris (2 m mu), kind 1 Monaghan artificial viscosity (m alpha c h, 0.01 h^2).
+template <typename T> struct Visc {
+    int kind;
+    T twomumass, avc, eh2;
+};
+template <typename T, typename IT> __device__ __forceinline__ Visc<T> visc_of(const IT &I)
+{
+    Visc<T> c;
+    c.kind = I.p.visc;
+    c.twomumass = I.p.twomumass;
+    c.avc = I.p.avc;
+    c.eh2 = I.p.eh2;
+    return c;
+}
+
+// accel_kernel!: a_i -= P F d, then a_i += C (v_i - v_j) (Morris), per
+// component. Artificial viscosity instead adds K d on approaching pairs,
+// K = avc s F / ((r^2 + eh2) (rho_i + rho_j) / 2), s = (v_i - v_j).d.
 template <typename T> struct AccelPair {
     T px, py, cx, cy;
 };
-template <typename T>
+template <typename T, bool AV = true>
 __device__ __forceinline__ AccelPair<T> accel_pair(T r2, T dx, T dy, T invh, T m, T Fc,
-                                                   T twomumass, T pti, T iri, const T2<T> &vi,
-                                                   const T2<T> &pj, const T2<T> &vj)
+                                                   const Visc<T> &vc, T pti, T iri, T rhoi,
+                                                   T rhoj, const T2<T> &vi, const T2<T> &pj,
+                                                   const T2<T> &vj)
 {
     const T q = pair_sqrt(r2) * invh;
     const T u = (T)1 - (T)0.5 * q;
@@ -305,9 +330,23 @@ __device__ __forceinline__ AccelPair<T> accel_pair(T r2, T dx, T dy, T invh, T m
     AccelPair<T> o;
     o.px = Pij * F * dx;
     o.py = Pij * F * dy;
-    const T C = twomumass * iri * pj.y * F;
-    o.cx = C * (vi.x - vj.x);
-    o.cy = C * (vi.y - vj.y);
+    if (AV && vc.kind == 1) {
+        const T wx = vi.x - vj.x;
+        const T wy = vi.y - vj.y;
+        const T s = wx * dx + wy * dy;
+        T K = (T)0;
+        if (s < (T)0) {
+            const T D = r2 + vc.eh2;
+            const T rb = (rhoi + rhoj) * (T)0.5;
+            K = vc.avc * s * F / (D * rb);
+        }
+        o.cx = K * dx;
+        o.cy = K * dy;
+    } else {
+        const T C = vc.twomumass * iri * pj.y * F;
+        o.cx = C * (vi.x - vj.x);
+        o.cy = C * (vi.y - vj.y);
+    }
     return o;
 }
 
@@ -316,12 +355,19 @@ __device__ __forceinline__ AccelPair<T> accel_pair(T r2, T dx, T dy, T invh, T m
 template <typename T> struct Pass1Pair {
     T gxs, gxa, gys, gya, gvx, gvy, grs, sS;
 };
-template <typename T>
+// With artificial viscosity the Morris terms vanish and the pair adds the
+// derivatives of (abar_i - abar_j).(K d): with A = (abar_i - abar_j).d,
+//   d/dd   = K da + A (K/s) w + A ((K/F) G/(h r) - 2K/D) d   (into gx, gy)
+//   d/dv_i = A (K/s) d                                        (into gvx, gvy)
+//   d/drho_i = -A K / (2 rb)                                  (into grho)
+template <typename T, bool AV = true>
 __device__ __forceinline__ Pass1Pair<T> pass1_pair(T r2, T dx, T dy, T invh, T m, T Fc, T Gc,
-                                                   T twomumass, T pti, T iri, const T2<T> &vi,
-                                                   const T2<T> &ab, const T2<T> &pj,
-                                                   const T2<T> &abj, const T2<T> &vj)
+                                                   const Visc<T> &vc, T pti, T iri, T rhoi,
+                                                   T rhoj, const T2<T> &vi, const T2<T> &ab,
+                                                   const T2<T> &pj, const T2<T> &abj,
+                                                   const T2<T> &vj)
 {
+    const T twomumass = vc.twomumass;
     T r, rinv;
     if constexpr (sizeof(T) == 4) {
         rinv = r2 > (T)0 ? rsqrtf(r2) : (T)0;
@@ -345,6 +391,38 @@ __device__ __forceinline__ Pass1Pair<T> pass1_pair(T r2, T dx, T dy, T invh, T m
     Pass1Pair<T> o;
     o.gxs = Pij * F * dax;
     o.gys = Pij * F * day;
+    if (AV && vc.kind == 1) {
+        const T s = dvx * dx + dvy * dy;
+        const T Fbar = Pij * ad_d;
+        T w;
+        if constexpr (sizeof(T) == 4) w = Fbar * G * invh * rinv;
+        else w = Fbar * G * invh / r;
+        const T Ad = dax * dx + day * dy;
+        T avx = (T)0, avy = (T)0, vx = (T)0, vy = (T)0, rs = (T)0;
+        if (s < (T)0) {
+            const T D = r2 + vc.eh2;
+            const T rb = (rhoi + rhoj) * (T)0.5;
+            const T Drb = D * rb;
+            const T K = vc.avc * s * F / Drb;
+            const T Ks = vc.avc * F / Drb;
+            const T KF = vc.avc * s / Drb;
+            T cd;
+            if constexpr (sizeof(T) == 4) cd = Ad * (KF * G * invh * rinv - (T)2 * K / D);
+            else cd = Ad * (KF * G * invh / r - (T)2 * K / D);
+            avx = K * dax + Ad * Ks * dvx + cd * dx;
+            avy = K * day + Ad * Ks * dvy + cd * dy;
+            vx = Ad * Ks * dx;
+            vy = Ad * Ks * dy;
+            rs = Ad * K / ((T)2 * rb);
+        }
+        o.gxa = w * dx + avx;
+        o.gya = w * dy + avy;
+        o.gvx = vx;
+        o.gvy = vy;
+        o.grs = rs;
+        o.sS = F * ad_d;
+        return o;
+    }
     const T Fbar = Pij * ad_d + Cbase * ad_v;
     T w;
     if constexpr (sizeof(T) == 4) w = Fbar * G * invh * rinv;
@@ -388,7 +466,8 @@ __device__ __forceinline__ T density_spill_sum(const NLView<T> &v, const IT &I, 
     return acc;
 }
 
-// Self term and eos_kernel!: rho = sum + m A, pterm = c^2 (rho - rho0) / rho^2.
+// Self term and eos_kernel!: rho = sum + m A, pterm = c^2 (rho - rho0) / rho^2
+// (Tait: B ((rho/rho0)^gamma - 1) / rho^2).
 template <typename T, typename IT>
 __device__ __forceinline__ void density_finish(const IT &I, int64_t i, T acc, T *__restrict__ rho,
                                                T2<T> *__restrict__ prho)
@@ -397,7 +476,10 @@ __device__ __forceinline__ void density_finish(const IT &I, int64_t i, T acc, T 
     const T ri = acc + m * A;
     if (rho) rho[i] = ri;
     const T inv = (T)1 / ri;
-    prho[i] = mk2<T>(I.p.c2 * (ri - I.p.rho0) * inv * inv, inv);
+    T pt;
+    if (I.p.eos == 1) pt = I.p.B * pow1m<T>((ri - I.p.rho0) / I.p.rho0, I.p.gam) * inv * inv;
+    else pt = I.p.c2 * (ri - I.p.rho0) * inv * inv;
+    prho[i] = mk2<T>(pt, inv);
 }
 
 // density_kernel! + eos_kernel!. It also records, for the rest of this step,
@@ -460,15 +542,18 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
 }
 
 // Pressure + Morris viscosity (accel_kernel! pair loop).
-template <typename T>
+template <typename T, bool AV = true>
 __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
                                           const T2<T> *__restrict__ vel,
-                                          const T2<T> *__restrict__ prho, int64_t i,
+                                          const T2<T> *__restrict__ prho,
+                                          const T *__restrict__ rho, int64_t i,
                                           const T2<T> &xi, const T2<T> &vi, T &ax, T &ay)
 {
-    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, twomumass = I.p.twomumass;
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc;
+    const Visc<T> vc = visc_of<T>(I);
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
+    const T rhoi = (AV && vc.kind == 1) ? rho[i] : (T)0;
     ax = (T)0;
     ay = (T)0;
     for_each_neighbor<T>(v, I, i, [&](int j) {
@@ -477,8 +562,9 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < r2max) {
-            const AccelPair<T> t =
-                accel_pair<T>(r2, dx, dy, invh, m, Fc, twomumass, pti, iri, vi, prho[j], vel[j]);
+            const T rhoj = (AV && vc.kind == 1) ? rho[j] : (T)0;
+            const AccelPair<T> t = accel_pair<T, AV>(r2, dx, dy, invh, m, Fc, vc, pti, iri, rhoi,
+                                                     rhoj, vi, prho[j], vel[j]);
             ax -= t.px;
             ay -= t.py;
             ax += t.cx;
@@ -495,10 +581,10 @@ __device__ __forceinline__ void accel_integrate_finish(
 
 // accel_kernel! (pressure + viscosity + gravity + wall, and alpha) fused with
 // integrate_kernel! (semi-implicit Euler, implicit Brinkman drag).
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool AV = false>
 __global__ void __launch_bounds__(kBlock)
     k_accel_integrate(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
-                      const T2<T> *__restrict__ prho,
+                      const T2<T> *__restrict__ prho, const T *__restrict__ rho,
                       const T *__restrict__ theta, T2<T> *__restrict__ posOut,
                       T2<T> *__restrict__ velOut, T2<T> *__restrict__ aOut,
                       T *__restrict__ alphaOut, uint32_t *__restrict__ flags)
@@ -510,7 +596,7 @@ __global__ void __launch_bounds__(kBlock)
     const T2<T> xi = v.pos[i];
     const T2<T> vi = vel[i];
     T ax, ay;
-    accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+    accel_sum<T, AV>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
     accel_integrate_finish<T>(I, b, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags);
 }
 
@@ -634,10 +720,10 @@ __device__ __forceinline__ int drag_adj_finish(const IT &I, int64_t i, const T2<
 // (gV += dt gX) + _adj_drag! (implicit Brinkman VJP). Also records, per
 // instance, the largest binary exponent of |galpha| for the exact theta
 // reduction (emax holds two slots per instance, selected by step parity).
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool AV = false>
 __global__ void __launch_bounds__(kBlock)
     k_accel_drag_adj(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
-                     const T2<T> *__restrict__ prho,
+                     const T2<T> *__restrict__ prho, const T *__restrict__ rho,
                      const T *__restrict__ theta, const T2<T> *__restrict__ gX,
                      T2<T> *__restrict__ gV, T2<T> *__restrict__ abar, T *__restrict__ galpha,
                      int *__restrict__ emax, int parity)
@@ -652,7 +738,7 @@ __global__ void __launch_bounds__(kBlock)
         const T2<T> xi = v.pos[i];
         const T2<T> vi = vel[i];
         T ax, ay;
-        accel_sum<T>(v, I, vel, prho, i, xi, vi, ax, ay);
+        accel_sum<T, AV>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
         e = drag_adj_finish<T>(I, i, xi, vi, ax, ay, theta, gX, gV, abar, galpha);
     }
     // max over the lanes of each instance present in the warp, one atomic each
@@ -668,17 +754,18 @@ __global__ void __launch_bounds__(kBlock)
     if ((int)lane_id() == __ffs(peers) - 1 && mx != INT_MIN) atomicMax(emax + 2 * b + parity, mx);
 }
 
-template <typename T, typename IT>
+template <typename T, bool AV, typename IT>
 __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64_t i,
                                           const T2<T> *__restrict__ vel,
                                           const T2<T> *__restrict__ prho,
+                                          const T *__restrict__ rho,
                                           const T2<T> *__restrict__ abar, const T2<T> &xi,
                                           const T2<T> &vi, const T2<T> &ab, const T2<T> &pi,
                                           T &gx, T &gy, T &gvx, T &gvy, T &grh, T &sumS);
 template <typename T, typename IT>
 __device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T> &xi,
-                                             const T2<T> &ab, const T2<T> &pi, T gx, T gy,
-                                             T gvx, T gvy, T grh, T sumS,
+                                             const T2<T> &ab, const T2<T> &pi, T rhoi, T gx,
+                                             T gy, T gvx, T gvy, T grh, T sumS,
                                              const T *__restrict__ theta,
                                              const T *__restrict__ galpha, T2<T> *__restrict__ gXs,
                                              T *__restrict__ grho, T2<T> *__restrict__ gV);
@@ -686,10 +773,10 @@ __device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T>
 // adj_pass1_kernel! (src/adjoint.jl:30-122) + the per-particle half of
 // adj_design_kernel! (gXs += galpha * grad alpha, src/adjoint.jl:173-175)
 // + _axpy2!(gV, gVs).
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool AV = false>
 __global__ void __launch_bounds__(kBlock)
     k_pass1_design(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
-                   const T2<T> *__restrict__ prho,
+                   const T2<T> *__restrict__ prho, const T *__restrict__ rho,
                    const T *__restrict__ theta, const T2<T> *__restrict__ abar,
                    const T *__restrict__ galpha, T2<T> *__restrict__ gXs, T *__restrict__ grho,
                    T2<T> *__restrict__ gV)
@@ -702,22 +789,26 @@ __global__ void __launch_bounds__(kBlock)
     const T2<T> ab = abar[i];
     const T2<T> pi = prho[i];
     T gx, gy, gvx, gvy, grh, sumS;
-    pass1_sum<T>(v, I, i, vel, prho, abar, xi, vi, ab, pi, gx, gy, gvx, gvy, grh, sumS);
-    pass1_finish<T>(I, i, xi, ab, pi, gx, gy, gvx, gvy, grh, sumS, theta, galpha, gXs, grho, gV);
+    pass1_sum<T, AV>(v, I, i, vel, prho, rho, abar, xi, vi, ab, pi, gx, gy, gvx, gvy, grh, sumS);
+    const T rhoi = I.p.eos == 1 || (AV && I.p.visc == 1) ? rho[i] : (T)0;
+    pass1_finish<T>(I, i, xi, ab, pi, rhoi, gx, gy, gvx, gvy, grh, sumS, theta, galpha, gXs, grho,
+                    gV);
 }
 
 // The pair loop of adj_pass1_kernel! (src/adjoint.jl:41-110).
-template <typename T, typename IT>
+template <typename T, bool AV, typename IT>
 __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64_t i,
                                           const T2<T> *__restrict__ vel,
                                           const T2<T> *__restrict__ prho,
+                                          const T *__restrict__ rho,
                                           const T2<T> *__restrict__ abar, const T2<T> &xi,
                                           const T2<T> &vi, const T2<T> &ab, const T2<T> &pi,
                                           T &gx, T &gy, T &gvx, T &gvy, T &grh, T &sumS)
 {
-    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc,
-            twomumass = I.p.twomumass;
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc;
+    const Visc<T> vc = visc_of<T>(I);
     const T pti = pi.x, iri = pi.y;
+    const T rhoi = (AV && vc.kind == 1) ? rho[i] : (T)0;
     gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
     for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
@@ -725,8 +816,9 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
         if (r2 < r2max) {
-            const Pass1Pair<T> t = pass1_pair<T>(r2, dx, dy, invh, m, Fc, Gc, twomumass, pti, iri,
-                                                 vi, ab, prho[j], abar[j], vel[j]);
+            const T rhoj = (AV && vc.kind == 1) ? rho[j] : (T)0;
+            const Pass1Pair<T> t = pass1_pair<T, AV>(r2, dx, dy, invh, m, Fc, Gc, vc, pti, iri,
+                                                     rhoi, rhoj, vi, ab, prho[j], abar[j], vel[j]);
             gx -= t.gxs;
             gy -= t.gys;
             gx += t.gxa;
@@ -743,8 +835,8 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
 // half of adj_design_kernel! and _axpy2!(gV, gVs).
 template <typename T, typename IT>
 __device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T> &xi,
-                                             const T2<T> &ab, const T2<T> &pi, T gx, T gy,
-                                             T gvx, T gvy, T grh, T sumS,
+                                             const T2<T> &ab, const T2<T> &pi, T rhoi, T gx,
+                                             T gy, T gvx, T gvy, T grh, T sumS,
                                              const T *__restrict__ theta,
                                              const T *__restrict__ galpha, T2<T> *__restrict__ gXs,
                                              T *__restrict__ grho, T2<T> *__restrict__ gV)
@@ -752,7 +844,8 @@ __device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T>
     const T pti = pi.x, iri = pi.y;
     const Phys<T> &p = I.p;
     grh += ((T)(-2) * p.m * pti * iri) * sumS;
-    grh += p.c2 * p.m * iri * iri * sumS;
+    if (p.eos == 1) grh += p.dB * pow_fold<T>(rhoi / p.rho0, p.gam - 1) * p.m * iri * iri * sumS;
+    else grh += p.c2 * p.m * iri * iri * sumS;
     gx += ab.x * wall_daccel<T>(xi.x, p.Lx, p.kw);
     gy += ab.y * wall_daccel<T>(xi.y, p.Ly, p.kw);
     T al, dadx, dady;
@@ -932,6 +1025,12 @@ __global__ void k_gather_theta(int64_t N, unsigned gridN, const int32_t *__restr
         theta_node<T>((int64_t)(blockIdx.x - gridN) * blockDim.x + threadIdx.x, nnode, B, inst,
                       acc, emax, parity, gtheta);
     }
+}
+
+static __global__ void k_fill_int(int64_t n, int *__restrict__ a, int v)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = v;
 }
 
 template <typename T>

@@ -229,6 +229,7 @@ class Server {
             p.h = r.p.h; p.m = r.p.m; p.rho0 = r.p.rho0; p.c = r.p.c; p.mu = r.p.mu;
             p.gx = r.p.gx; p.gy = r.p.gy; p.dt = r.p.dt; p.Lx = r.p.Lx; p.Ly = r.p.Ly;
             p.kw = r.p.kw; p.ngx = r.p.ngx; p.ngy = r.p.ngy;
+            p.eos = r.p.eos; p.gamma = r.p.gamma; p.visc = r.p.visc; p.alpha = r.p.alpha;
             const NLOpts o{r.skin, r.interval, r.maxnb};
             const std::vector<Params> ps{p};
             const std::vector<int64_t> ns{r.N};
