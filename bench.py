@@ -203,7 +203,15 @@ def run_batched(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / reps, (L.sph_launch_count() - n0) / reps
 
-    ms_b, launches_b = timed(solve_batch, args.steps)
+    graph = None
+    if args.graph:
+        # the whole batched solve recorded once as a CUDA graph, replayed per step
+        for _ in range(max(1, args.warmup)):
+            solve_batch()
+        torch.cuda.synchronize()
+        graph = S.capture(solve_batch)
+    ms_b, launches_b = timed(graph.launch if graph is not None else solve_batch, args.steps)
+    graph = None
     del tape
 
     # the same instances, one solve at a time
@@ -238,7 +246,8 @@ def run_batched(args):
             "dtype": args.dtype, "data": "synthetic", "config": cfg,
             "plain": {"value": ps_total / (ms_p / 1000.0), "ms_per_step": ms_p,
                       "gpu_launches_per_step": launches_p},
-            "speedup_vs_plain": ms_p / ms_b, "gpu_launches": launches_b}
+            "speedup_vs_plain": ms_p / ms_b, "gpu_launches": launches_b,
+            "graph": bool(args.graph)}
     print(json.dumps(line))
 
 
@@ -709,7 +718,7 @@ def main():
                     choices=["single", "small", "dense", "batched", "served"])
     ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
     ap.add_argument("--rates", default="10,100,500", help="served: arrival rates (1/s)")
-    ap.add_argument("--workers", type=int, default=6, help="served: concurrent requests")
+    ap.add_argument("--workers", type=int, default=12, help="served: concurrent requests")
     ap.add_argument("--hbm-budget-gb", type=float, default=96.0, help="served: admission budget")
     ap.add_argument("--instances", type=int, default=64, help="batched: number of instances")
     ap.add_argument("--model", default="reference", choices=sorted(MODELS),

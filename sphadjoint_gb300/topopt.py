@@ -118,41 +118,37 @@ class Problem:
     filt_r: int = 2
     interval: int = 2
     snapshots: int = 0
+
+    use_graphs: bool = True
     filt: DensityFilter = field(init=False)
 
     def __post_init__(self):
         self.filt = DensityFilter(self.p.ngy, self.p.ngx, self.filt_r)
         self.N = int(np.asarray(self.X0).size // 2)
+        self._solver = None
 
     def theta_of(self, rd):
         return alpha_of(self.filt.apply(rd), self.alpha_max, self.qp)
+
+    def _solve(self, theta, grad):
+        """J (and dJ/dtheta) of one design: objects made once per problem, the
+        two solve sequences captured as CUDA graphs on first use and replayed
+        with the new design written into the same device field."""
+        if self._solver is None:
+            self._solver = _Solver(self)
+        return self._solver.run(theta, grad)
 
     def objective_and_grad(self, rd):
         """J and dJ/drd: filter -> alpha -> simulate -> target_objective ->
         backward -> d alpha/d rho -> filter adjoint."""
         rdf = self.filt.apply(rd)
         theta = alpha_of(rdf, self.alpha_max, self.qp)
-        st = S.State(self.X0, self.V0, self.p, interval=self.interval)
-        tape = S.Tape(self.N, self.nsteps, self.p, snapshots=self.snapshots)
-        th = S.DesignField(theta, self.p.dtype)
-        S.simulate(st, th, self.p, self.nsteps, tape)
-        X, _ = st.get()
-        J, seed = S.target_objective(np.asarray(X, np.float64), self.target[0], self.target[1],
-                                     self.sigma)
-        ws = S.AdjointWorkspace(self.N, self.p)
-        S.backward(ws, tape, th, self.p, seed, np.zeros_like(seed), interval=self.interval)
-        gtheta = np.asarray(ws.get()[2], np.float64)
+        J, gtheta = self._solve(theta, grad=True)
         grdf = gtheta * dalpha_of(rdf, self.alpha_max, self.qp)
-        return float(J), self.filt.adjoint(grdf)
+        return J, self.filt.adjoint(grdf)
 
     def objective_only(self, rd):
-        theta = self.theta_of(rd)
-        st = S.State(self.X0, self.V0, self.p, interval=self.interval)
-        S.simulate(st, S.DesignField(theta, self.p.dtype), self.p, self.nsteps)
-        X, _ = st.get()
-        J, _ = S.target_objective(np.asarray(X, np.float64), self.target[0], self.target[1],
-                                  self.sigma)
-        return float(J)
+        return self._solve(self.theta_of(rd), grad=False)[0]
 
     def objectives_concurrent(self, server, rds):
         """objective_only for several designs at once: forward-only requests on
@@ -162,6 +158,51 @@ class Problem:
                                  args=(self.target[0], self.target[1], self.sigma),
                                  interval=self.interval, adjoint=False) for rd in rds]
         return [t.wait()["J"] for t in tickets]
+
+
+class _Solver:
+    """Device objects of one Problem and its two captured solves: forward +
+    target objective, and forward (taped) + target objective + seeded
+    backward. Each starts from a pristine copy of the initial state, so a
+    replay repeats the whole solve for whatever design the field holds."""
+
+    def __init__(self, prob: Problem):
+        self.prob = prob
+        p, n = prob.p, prob.nsteps
+        self.st0 = S.State(prob.X0, prob.V0, p, interval=prob.interval)
+        self.st = S.State(prob.X0, prob.V0, p, interval=prob.interval)
+        self.th = S.DesignField(np.zeros((p.ngy, p.ngx)), p.dtype)
+        self.tp = S.Tape(prob.N, n, p, snapshots=prob.snapshots)
+        self.ws = S.AdjointWorkspace(prob.N, p)
+        self.args = (prob.target[0], prob.target[1], prob.sigma)
+        self.graphs = {}
+
+    def _forward(self, tape):
+        pr = self.prob
+        self.st.assign(self.st0)
+        if tape is not None:
+            S.reset(tape)
+        S.simulate(self.st, self.th, pr.p, pr.nsteps, tape)
+        self.ws.objective(self.st, "target", self.args)
+
+    def _grad(self):
+        self._forward(self.tp)
+        S.backward_seeded(self.ws, self.tp, self.th, self.prob.p, interval=self.prob.interval)
+
+    def run(self, theta, grad):
+        self.th.upload(theta)
+        fn = self._grad if grad else (lambda: self._forward(None))
+        if not self.prob.use_graphs:
+            fn()
+        elif grad in self.graphs:
+            self.graphs[grad].launch()
+            S.synchronize()
+        else:
+            fn()  # first run allocates; then record it
+            self.graphs[grad] = S.capture(fn)
+        J = self.ws.objective_value()
+        gt = np.asarray(self.ws.get()[2], np.float64) if grad else None
+        return J, gt
 
 
 def optimize(prob: Problem, rd0=None, maxit=40, step0=0.05, server=None, log=None):
