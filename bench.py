@@ -640,6 +640,37 @@ def run_ours(args):
                 kernels[k] = {"ms": round(a.value, 3), "launches": b.value}
             L.sph_profile_enable(LB.KERNEL_ID[k], 0)
 
+    # the same solve in FP64 on the GPU (the FP64 oracle run of the workload):
+    # relative difference of the FP32 results, max |a - b| / max |b|
+    fp64 = None
+    if args.fp64_check and args.dtype == "f32" and rank == 0:
+        def grab(st_, ws_):
+            X_, V_ = st_.get()
+            gX_, gV_, gt_ = ws_.get()
+            return {k: np.asarray(a, np.float64) for k, a in
+                    (("X", X_), ("V", V_), ("gX", gX_), ("gV", gV_), ("gtheta", gt_))}
+
+        solve()
+        torch.cuda.synchronize()
+        r32 = grab(st, ws)
+        J32 = J.value
+        p64 = S.SPHParams(**p_d, dtype="f64")
+        st64 = S.State(X0, V0, p64, interval=interval)
+        th64 = S.DesignField(theta, "f64")
+        tp64 = S.Tape(N, args.nsteps, p64, snapshots=args.snapshots)
+        ws64 = S.AdjointWorkspace(N, p64)
+        t0 = time.perf_counter()
+        S.simulate(st64, th64, p64, args.nsteps, tp64)
+        J64 = ws64.objective(st64, "ke_right")
+        S.backward_seeded(ws64, tp64, th64, p64, interval=interval)
+        r64 = grab(st64, ws64)
+        fp64 = {"seconds": time.perf_counter() - t0, "J_f32": J32, "J_f64": J64,
+                "J_rel": abs(J32 - J64) / abs(J64)}
+        for k in r64:
+            fp64[k + "_rel"] = float(np.max(np.abs(r32[k] - r64[k])) /
+                                     max(np.max(np.abs(r64[k])), 1e-300))
+        del st64, tp64, ws64
+
     # e2e: the reference-facing calls with host buffers
     e2e = None
     if args.e2e_steps > 0:
@@ -701,7 +732,7 @@ def run_ours(args):
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk,
                 "recomputed_forward_steps_per_solve": rec,
                 "objective_J": J.value, "kernels_one_solve": kernels,
-                "block_sizes": blocks, "graph": graph is not None,
+                "block_sizes": blocks, "fp64_check": fp64, "graph": graph is not None,
                 "graph_kernels_per_solve": graph.nodes if graph is not None else None}
         print(json.dumps(line))
     if world > 1:
@@ -741,6 +772,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--breakdown", type=int, default=1)
+    ap.add_argument("--fp64-check", type=int, default=0,
+                    help="also solve the workload in FP64 on the GPU and report the FP32 "
+                         "results' relative difference")
     ap.add_argument("--graph", type=int, default=0,
                     help="time replays of the whole solve captured as one CUDA graph")
     ap.add_argument("--autotune", type=int, default=1,

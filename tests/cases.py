@@ -118,3 +118,23 @@ def ke_seeds(X, V, p):
 def relerr(a, b):
     a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def jittered_block_case(side=64, ntheta=32, seed=1):
+    """The benchmark's single-instance workload at a smaller side: a side x side
+    lattice, dx = 1e-3, jitter U(+-0.05 dx), h = 1.3 dx, rho0 = 1000,
+    c0 = 10 sqrt(2 g H), dt = 0.25 h / c0, tank 2H x 1.25H, smoothed theta."""
+    dx = 1e-3
+    H = side * dx
+    h = 1.3 * dx
+    c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+    p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0,
+             Lx=2.0 * H, Ly=1.25 * H, kw=5e4, ngx=ntheta, ngy=ntheta)
+    rng = np.random.default_rng(seed)
+    xs = dx + dx * np.arange(side)
+    X, Y = np.meshgrid(xs, xs)
+    X0 = np.vstack([X.ravel(), Y.ravel()]) + rng.uniform(-0.05 * dx, 0.05 * dx, (2, side * side))
+    t = np.random.default_rng(seed + 1).random((ntheta, ntheta))
+    pad = np.pad(t, 2, mode="edge")
+    theta = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
+    return dict(p=p, X0=X0, V0=np.zeros_like(X0), theta=theta)
