@@ -764,9 +764,9 @@ def main():
     ap.add_argument("--kernel-events", type=int, default=1,
                     help="time --kernel with CUDA events inside the timed region (1) or on "
                          "one extra solve after it (0)")
-    ap.add_argument("--traffic-bytes", type=float, default=81.05e6,
+    ap.add_argument("--traffic-bytes", type=float, default=81.09e6,
                     help="ncu dram read+write bytes of one launch of --kernel at the default "
-                         "size (k_pass1_design, 1,048,576 particles: 76.11 MB + 4.94 MB), "
+                         "size (k_pass1_design, 1,048,576 particles: 76.1 MB + 5.0 MB), "
                          "reported as roofline.traffic; 0 = unknown")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
