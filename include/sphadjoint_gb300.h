@@ -280,13 +280,14 @@ SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_
 
 /* Lanes per particle of the neighbour-list and pair-sum kernels (no
    counterpart in the reference), process-wide. 0 (default): by state size --
-   FP64 single states of up to 16384 particles give each particle a group of
-   32 lanes (up to 512 particles) or 16 lanes, everything else one thread.
-   1: always one thread. 16 or 32: groups for every single-instance state.
-   Every setting adds each particle's pair terms in the same order, so FP64
-   results are bit-identical across settings; FP32 results may differ in the
-   last bits (multiply-add contraction differs between the forms). Batches
-   always use one thread per particle. Other values: SPH_ERR_ARG. */
+   single states of up to 16384 particles give each particle a group of 32
+   lanes (up to 512 particles in FP64, 2048 in FP32) or 16 lanes, larger
+   states one thread. 1: always one thread. 16 or 32: groups for every
+   single-instance state. Every setting adds each particle's pair terms in the
+   same order, so FP64 results are bit-identical across settings; FP32 results
+   may differ in the last bits (multiply-add contraction differs between the
+   forms). Batches always use one thread per particle, so an FP32 batch member
+   equals a solo run made with lanes = 1. Other values: SPH_ERR_ARG. */
 SPH_API int32_t sph_set_group_lanes(int32_t lanes);
 SPH_API int32_t sph_get_group_lanes(int32_t *lanes);
 

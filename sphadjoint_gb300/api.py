@@ -623,9 +623,10 @@ def synchronize():
 
 def set_group_lanes(lanes: int) -> None:
     """Lanes per particle of the pair-sum kernels, process-wide (no counterpart
-    in the reference): 0 = by state size (default), 1 = one thread per
-    particle, 16 or 32 = a lane group per particle for single states. FP64
-    results are bit-identical across settings."""
+    in the reference): 0 = by state size (default: lane groups for single
+    states of up to 16384 particles), 1 = one thread per particle, 16 or 32 =
+    a lane group per particle for single states. FP64 results are
+    bit-identical across settings; FP32 results differ in the last bits."""
     L.check(L.load().sph_set_group_lanes(int(lanes)))
 
 

@@ -137,15 +137,18 @@ template <typename T> int &tuned_block(int kid, bool multi)
         }                                                                                     \
     } while (0)
 
-// FP64 single states up to this many particles use lane groups by default:
-// one thread per particle would leave most SMs idle on the slow FP64 pipe.
-// Kernel time per fwd+adjoint step (density .. pass 2), one thread / 16 /
-// 32 lanes: 240 particles 538 / 112 / 100 us, 1024: 560 / 112 / 123 us,
-// 2072: 110 (pass 1 alone) / 30 / 42 us, 8288: 555 / 346 / 501 us. 32 lanes
-// win only for a few hundred particles, where the critical path of one
-// group matters more than the total work.
+// Single states up to this many particles use lane groups by default: one
+// thread per particle leaves most SMs idle (and, in FP64, bound by the slow
+// FP64 pipe on the few SMs it uses). Kernel time per fwd+adjoint step,
+// one thread / 16 / 32 lanes:
+//   FP64: 240 particles 538 / 112 / 100 us, 1024: 560 / 112 / 123 us,
+//         8288: 555 / 346 / 501 us;
+//   FP32: 240 particles 99 / 78 / 73 us, 1024: 110 / 81 / 74 us,
+//         2072: 115 / 82 / 79 us, 8288: 125 / 107 / 137 us.
+// 32 lanes win only for small states, where the critical path of one group
+// matters more than the total work.
 constexpr int64_t kCoopMaxN = 16384;
-constexpr int64_t kCoop32MaxN = 512;
+template <typename T> constexpr int64_t coop32_max_n() { return sizeof(T) == 8 ? 512 : 2048; }
 
 // Constants formed in T exactly as the reference kernels form them.
 template <typename T> Phys<T> make_phys(const Params &q)
@@ -454,8 +457,8 @@ template <typename T> class Sys final : public StateI {
         if (B != 1) return 0;
         const int f = rt_group_lanes();
         if (f == 16 || f == 32) return f;
-        if (f == 1 || sizeof(T) != 8 || N_ > kCoopMaxN) return 0;
-        return N_ <= kCoop32MaxN ? 32 : 16;
+        if (f == 1 || N_ > kCoopMaxN) return 0;
+        return N_ <= coop32_max_n<T>() ? 32 : 16;
     }
 
     void upload_inst()

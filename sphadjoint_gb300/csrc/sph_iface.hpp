@@ -83,7 +83,7 @@ void rt_before_launch(int kid);
 void rt_after_launch(int kid);
 void rt_check_launch(const char *name);
 // Lanes per particle of the pair-sum kernels: 0 = by state size (groups of 16
-// or 32 lanes for FP64 states of up to 16384 particles, one thread otherwise), 1 = one thread,
+// or 32 lanes for single states of up to 16384 particles, one thread otherwise), 1 = one thread,
 // 16 or 32 = groups for every single-instance state.
 int rt_group_lanes();
 void rt_set_group_lanes(int lanes);
