@@ -138,3 +138,26 @@ def jittered_block_case(side=64, ntheta=32, seed=1):
     pad = np.pad(t, 2, mode="edge")
     theta = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
     return dict(p=p, X0=X0, V0=np.zeros_like(X0), theta=theta)
+
+
+def dense_block_case(side=2896, ntheta=512, seed=5):
+    """The benchmark's dense stress workload: a side x side block compressed
+    1.15x (spacing dx / 1.15, mass of the uncompressed lattice), theta with
+    50% solid blobs (1000 vs 0)."""
+    dx = 1e-3
+    sp = dx / 1.15
+    H = side * sp
+    h = 1.3 * dx
+    c0 = 10.0 * math.sqrt(2 * 9.81 * H)
+    p = dict(h=h, m=1000.0 * dx * dx, rho0=1000.0, c=c0, mu=0.02, dt=0.25 * h / c0,
+             Lx=2.0 * H, Ly=1.25 * H, kw=5e4, ngx=ntheta, ngy=ntheta)
+    rng = np.random.default_rng(seed)
+    xs = sp + sp * np.arange(side)
+    X, Y = np.meshgrid(xs, xs)
+    X0 = np.vstack([X.ravel(), Y.ravel()]) + rng.uniform(-0.05 * sp, 0.05 * sp, (2, side * side))
+    f = rng.standard_normal((ntheta, ntheta))
+    for _ in range(6):
+        pad = np.pad(f, 2, mode="wrap")
+        f = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
+    theta = np.where(f > np.median(f), 1000.0, 0.0)
+    return dict(p=p, X0=X0, V0=np.zeros_like(X0), theta=theta)
