@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU parity oracle (test infrastructure only).
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` use this module, and only as the checker (or the timed CPU
+``bench.py`` use this module, and only as the parity reference (or the timed CPU
 baseline). The product (``sphadjoint_gb300``) never imports it.
 
 The oracle restates the reference Julia package SPHAdjoint (src/*.jl) in C;
