@@ -473,7 +473,9 @@ __device__ __forceinline__ void density_finish(const IT &I, int64_t i, T acc, T 
                                                T2<T> *__restrict__ prho)
 {
     const T m = I.p.m, A = I.p.A;
-    const T ri = acc + m * A;
+    // explicit roundings: the same result whichever kernel form inlines this
+    // (a multiply-add contraction here would depend on the surrounding code)
+    const T ri = add_rn(acc, mul_rn(m, A));
     if (rho) rho[i] = ri;
     const T inv = (T)1 / ri;
     T pt;
@@ -547,7 +549,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
                 acc += density_pair<T>(r2, invh, m, A);
             }
         }
-        if constexpr (sizeof(T) == 4) acc = m * A * acc;
+        if constexpr (sizeof(T) == 4) acc = mul_rn(mul_rn(m, A), acc);
     } else {
         acc = density_spill_sum<T>(v, I, i, xi, tmaskOut);
     }
