@@ -83,6 +83,15 @@ class SPHParams:
         return self.Ly / (self.ngy - 1)
 
 
+def _check_layout(layout):
+    """NeighborList's index layout (src/neighbors.jl:178-184): :auto, :slot or
+    :particle. The library keeps its own per-particle row masks in every case
+    (results do not depend on the layout); sph_get_neighbors returns rows in
+    the particle-major form."""
+    if str(layout).lstrip(":") not in ("auto", "slot", "particle"):
+        raise L.ArgumentError(1, "layout must be :slot, :particle or :auto")
+
+
 def _xy(a, N, dt):
     """(2, N) or (N, 2) -> contiguous (N, 2) of T (the interleaved layout)."""
     a = np.asarray(a)
@@ -131,7 +140,8 @@ def _field(theta, p: SPHParams) -> DesignField:
 class State:
     """State(backend, X0, V0, p; skin, interval, maxnb) (src/driver.jl:24-36)."""
 
-    def __init__(self, X0, V0, p: SPHParams, skin=0.2, interval=4, maxnb=64):
+    def __init__(self, X0, V0, p: SPHParams, skin=0.2, interval=4, maxnb=64, layout="auto"):
+        _check_layout(layout)
         self._L = L.load()
         self.p = p
         self.N = N = int(np.asarray(X0).size // 2)
@@ -574,9 +584,11 @@ def simulate(st: State, theta, p: SPHParams | None, nsteps: int, tape: Tape | No
 
 
 def backward(ws: AdjointWorkspace, tape: Tape, theta, p: SPHParams, seedX, seedV=None,
-             scratch: State | None = None, skin=0.2, interval=4, maxnb=64) -> AdjointWorkspace:
+             scratch: State | None = None, skin=0.2, interval=4, maxnb=64,
+             layout="auto") -> AdjointWorkspace:
     """backward!(ws, tape, theta, p, backend; seedX, seedV, scratch, skin,
-    interval, maxnb) (src/driver.jl:141-207)."""
+    interval, maxnb, layout) (src/driver.jl:141-207)."""
+    _check_layout(layout)
     th = _field(theta, p)
     N = ws.N
     sx = _xy(seedX, N, p.np) if seedX is not None else None

@@ -68,3 +68,13 @@ def test_checkpoint_schedule_is_optimal(lib, c):
 def test_checkpoint_cost_of_the_benchmark_horizon(lib):
     # 1000 steps, 32 snapshots: repetition number 3, 3*1000 - C(35, 2) = 2405
     assert lib.sph_plan_cost(1000, 32) == 2405
+
+
+def test_layout_keyword_is_validated_like_the_reference():
+    # src/neighbors.jl:178-184: :slot / :particle / :auto, else ArgumentError
+    import sphadjoint_gb300.api as A
+    import sphadjoint_gb300._lib as LB
+    for ok in ("auto", ":slot", "particle"):
+        A._check_layout(ok)
+    with pytest.raises(LB.ArgumentError):
+        A._check_layout("columns")
