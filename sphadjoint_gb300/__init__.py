@@ -4,6 +4,8 @@
 reference's Julia API over that ABI."""
 from .api import (  # noqa: F401
     AdjointWorkspace,
+    CellList,
+    NeighborList,
     Batch,
     BatchField,
     BatchWorkspace,

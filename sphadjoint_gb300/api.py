@@ -552,14 +552,90 @@ def reset(tape: Tape) -> Tape:
     return tape.reset()
 
 
-def build(st: State) -> State:
-    """build!(cl, X, p, backend) (src/neighbors.jl:97-114)."""
+def _skin_for(cs: float, p: SPHParams) -> float:
+    """The neighbour-list skin whose cutoff Float64(support(p)) * (1 + skin)
+    equals cs exactly (the library's cell width is that cutoff)."""
+    s = float(p.np(2) * p.np(p.h))
+    skin = cs / s - 1.0
+    for _ in range(64):
+        rc = s * (1.0 + skin)
+        if rc == cs:
+            return skin
+        skin = np.nextafter(skin, np.inf if rc < cs else -np.inf)
+    raise L.ArgumentError(1, f"cell width {cs!r} is not reachable as 2h(1 + skin)")
+
+
+class CellList:
+    """CellList(backend, N, p; cs = support(p)) (src/neighbors.jl:9-36) as a
+    standalone object: after build(cl, X) it holds counts, starts (0-based),
+    order (1-based ids) and cellof of the positions X, bit for bit as the
+    reference computes them. cs must be at least the support 2h."""
+
+    def __init__(self, N: int, p: SPHParams, cs=None):
+        self.N, self.p = int(N), p
+        self.cs = float(cs) if cs is not None else float(p.np(2) * p.np(p.h))
+        self._skin = _skin_for(self.cs, p)
+        self.nx = max(1, int(np.ceil(float(p.np(p.Lx)) / self.cs)) + 2)
+        self.ny = max(1, int(np.ceil(float(p.np(p.Ly)) / self.cs)) + 2)
+        self.counts = self.starts = self.order = None
+
+
+class NeighborList:
+    """NeighborList(backend, N, p; skin, interval, maxnb, layout)
+    (src/neighbors.jl:150-190) as a standalone object: after
+    build_neighbors(nl, cl, X) it holds indices (particle-major, 1-based ids,
+    shape (N, maxnb)), counts and flags, and age = 0."""
+
+    def __init__(self, N: int, p: SPHParams, skin=0.2, interval=4, maxnb=64, layout="auto"):
+        _check_layout(layout)
+        self.N, self.p = int(N), p
+        self.skin, self.interval, self.maxnb = float(skin), int(interval), int(maxnb)
+        self.rc = float(p.np(2) * p.np(p.h)) * (1.0 + self.skin)
+        self.age = np.iinfo(np.int64).max
+        self.indices = self.counts = None
+        self.flags = 0
+        self._st = None
+
+
+def build(st, X=None, p: SPHParams | None = None, backend=None):
+    """build!(cl, X, p, backend) (src/neighbors.jl:97-114): the cell list of a
+    State's current positions, or of positions X into a standalone CellList."""
+    if isinstance(st, CellList):
+        cl = st
+        if X is None:
+            raise L.ArgumentError(1, "build(cl, X): positions are required")
+        s = State(X, np.zeros_like(np.asarray(X, np.float64)), p or cl.p, skin=cl._skin)
+        L.check(s._L.sph_build_cells(s.h))
+        c = s.celllist()
+        cl.counts, cl.starts, cl.order = c["counts"], c["starts"], c["order"]
+        return cl
     L.check(st._L.sph_build_cells(st.h))
     return st
 
 
-def build_neighbors(st: State) -> State:
-    """build_neighbors!(nl, cl, X, p, backend) (src/neighbors.jl:252-263)."""
+def build_neighbors(st, cl: CellList | None = None, X=None, p: SPHParams | None = None,
+                    backend=None):
+    """build_neighbors!(nl, cl, X, p, backend) (src/neighbors.jl:252-263): on
+    a State, or into a standalone NeighborList (and its CellList) from
+    positions X; the displacement check runs against the previous build."""
+    if isinstance(st, NeighborList):
+        nl = st
+        if X is None:
+            raise L.ArgumentError(1, "build_neighbors(nl, cl, X): positions are required")
+        pp = p or nl.p
+        if nl._st is None:
+            nl._st = State(X, np.zeros_like(np.asarray(X, np.float64)), pp, skin=nl.skin,
+                           interval=nl.interval, maxnb=nl.maxnb)
+        else:
+            nl._st.set(X=X)
+        L.check(nl._st._L.sph_build_neighbors(nl._st.h))
+        nl.indices, nl.counts = nl._st.neighbors()
+        nl.flags |= nl._st.take_flags()
+        nl.age = 0
+        if cl is not None:
+            c = nl._st.celllist()
+            cl.counts, cl.starts, cl.order = c["counts"], c["starts"], c["order"]
+        return nl
     L.check(st._L.sph_build_neighbors(st.h))
     return st
 

@@ -234,3 +234,28 @@ def test_fp32_error_on_the_benchmark_workload_is_ieee_fp32_error():
     for k in ("X", "V", "gX", "gV", "gtheta"):
         ieee = K.relerr(r32[k], r64[k])
         assert K.relerr(g32[k], r64[k]) <= 4 * ieee + 1e-6, (k, ieee)
+
+
+def test_standalone_celllist_and_neighborlist_match_oracle():
+    # CellList(backend, N, p; cs = support(p)) + build!, NeighborList + build_neighbors!
+    case = K.random_points_case()
+    p = S.SPHParams(**case["p"])
+    X = case["X0"]
+    cl = S.CellList(X.shape[1], p)
+    S.build(cl, X)
+    o = O.Oracle("f64")
+    ost = o.state(O.params(**case["p"]), X, case["V0"], skin=0.0)
+    ost.build_cells()
+    c = ost.cells()
+    for k in ("counts", "starts", "order"):
+        assert np.array_equal(getattr(cl, k), c[k]), k
+    nl = S.NeighborList(X.shape[1], p, skin=0.2, layout="slot")
+    cl2 = S.CellList(X.shape[1], p, cs=nl.rc)
+    S.build_neighbors(nl, cl2, X)
+    ost2 = o.state(O.params(**case["p"]), X, case["V0"], skin=0.2)
+    ost2.build_neighbors(case["p"]["h"])
+    oi, on = ost2.neighbors()
+    assert nl.age == 0 and np.array_equal(nl.counts, on)
+    for i in range(X.shape[1]):
+        assert np.array_equal(nl.indices[i, : nl.counts[i]], oi[i, : on[i]]), i
+    assert np.array_equal(cl2.order, ost2.cells()["order"])
