@@ -259,3 +259,31 @@ def test_standalone_celllist_and_neighborlist_match_oracle():
     for i in range(X.shape[1]):
         assert np.array_equal(nl.indices[i, : nl.counts[i]], oi[i, : on[i]]), i
     assert np.array_equal(cl2.order, ost2.cells()["order"])
+
+
+@pytest.mark.parametrize("lanes", [1, 32])
+def test_step_by_step_fields_match_oracle(lanes):
+    """step! one step at a time, reading every step's density, pterm, 1/rho,
+    acceleration a_rest and Brinkman alpha (keep_accel), against the oracle's
+    arrays after each step (FP64, bit for bit)."""
+    S.set_group_lanes(lanes)
+    try:
+        case = K.adjoint_case(seed=9)
+        p, st, o, ost = _states(case, interval=2)
+        st.keep_accel(True)
+        th = S.DesignField(case["theta"])
+        oth = o.theta(case["theta"])
+        op = O.params(**case["p"])
+        for n in range(6):
+            S.step(st, th, p)
+            o.step(ost, oth, op)
+            g = st.fields(accel=True)
+            r = ost.fields()
+            for k in ("rho", "pterm", "invrho", "alpha"):
+                assert np.array_equal(g[k], r[k]), (n, k)
+            assert np.array_equal(np.asarray(g["a"]).T, r["a"]), n
+            X, V = st.get()
+            oX, oV = ost.get()
+            assert np.array_equal(np.asarray(X).T, oX) and np.array_equal(np.asarray(V).T, oV)
+    finally:
+        S.set_group_lanes(0)
