@@ -9,7 +9,9 @@
 //   prho                              : T2 {p/rho^2, 1/rho} per particle
 //   perm / invperm                    : int32 slot -> particle id / id -> slot
 //   center                            : uint32 per particle (cx | cy<<16 | spill<<31)
-//   masks                             : 3 x uint64 per particle, row-major by row
+//   masks, tmask                      : 6 x uint32 per particle, word-major
+//                                       (masks[w * N + i]; row r = words 2r, 2r+1);
+//                                       tmask: this step's in-support subset
 //   cellStart                         : int32 x (ncell + 1)
 // Reference kernels restated: src/neighbors.jl:44-80,192-245 (cell list and
 // neighbour list), src/forward.jl:25-147, src/adjoint.jl:30-228.
