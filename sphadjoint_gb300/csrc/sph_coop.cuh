@@ -298,7 +298,8 @@ __global__ void __launch_bounds__(kCoopBlock)
                            const T *__restrict__ theta,
                            T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
                            T2<T> *__restrict__ aOut, T *__restrict__ alphaOut,
-                           uint32_t *__restrict__ flags)
+                           uint32_t *__restrict__ flags, const int32_t *__restrict__ perm,
+                           T2<T> *__restrict__ tx, T2<T> *__restrict__ tv)
 {
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][4][G];
@@ -317,7 +318,8 @@ __global__ void __launch_bounds__(kCoopBlock)
         accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, rho, xi, vi, ax, ay);
         if (g.gl != 0) return;
     }
-    accel_integrate_finish<T>(I, 0, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags);
+    accel_integrate_finish<T>(I, 0, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags,
+                              perm, tx, tv);
 }
 
 // Accel recompute + _adj_integrate! + _adj_drag!; one exponent update per

@@ -670,7 +670,8 @@ template <typename T> class Sys final : public StateI {
     {
         maybe_rebuild();
         if (N_ == 0) return;
-        if (tx) SPH_LAUNCH(K_TAPE, k_tape_store<T>, N_, N_, perm.p, pos[cur].p, vel[cur].p, tx, tv);
+        // the tape slot (tx, tv) is written by the accel pass from the same
+        // pre-step state it reads
         NLView<T> v = view();
         const int nxt = 1 - cur;
         T2<T> *aO = keepAccel ? accOut.p : (T2<T> *)nullptr;
@@ -681,7 +682,7 @@ template <typename T> class Sys final : public StateI {
             v.tmask = tmask.p;
             auto ki = G == 32 ? &k_accel_integrate_coop<T, 32> : &k_accel_integrate_coop<T, 16>;
             SPH_LAUNCH_COOP(K_ACCEL_INTEGRATE, G, ki, N_, v, vel[cur].p, prho.p, rho.p, theta,
-                            pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
+                            pos[nxt].p, vel[nxt].p, aO, alO, flags.p, perm.p, tx, tv);
         } else {
             auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
             SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rho.p, prho.p, tmask.p);
@@ -689,7 +690,7 @@ template <typename T> class Sys final : public StateI {
             auto ki = B > 1 ? (anyAV ? &k_accel_integrate<T, true, true> : &k_accel_integrate<T, true>)
                             : (anyAV ? &k_accel_integrate<T, false, true> : &k_accel_integrate<T, false>);
             SPH_LAUNCH_TUNED(K_ACCEL_INTEGRATE, B > 1, ki, N_, v, vel[cur].p, prho.p, rho.p,
-                             theta, pos[nxt].p, vel[nxt].p, aO, alO, flags.p);
+                             theta, pos[nxt].p, vel[nxt].p, aO, alO, flags.p, perm.p, tx, tv);
         }
         cur = nxt;
     }
@@ -1313,7 +1314,8 @@ template <typename T> class Tuner {
         v.tmask = S.tmask.p;
         b = timeit([&](int c) {
             ki<<<grid(c), c, 0, st>>>(v, S.vel[S.cur].p, S.prho.p, S.rho.p, th.th.p, S.pos[nxt].p,
-                                      S.vel[nxt].p, nullptr, nullptr, S.flags.p);
+                                      S.vel[nxt].p, nullptr, nullptr, S.flags.p, nullptr, nullptr,
+                                      nullptr);
         });
         tuned_block<T>(K_ACCEL_INTEGRATE, multi) = b;
         // adjoint passes on placeholder gradients

@@ -594,7 +594,8 @@ template <typename T, typename IT>
 __device__ __forceinline__ void accel_integrate_finish(
     const IT &I, int b, int64_t i, const T2<T> &xi, const T2<T> &vi, T ax, T ay,
     const T *__restrict__ theta, T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
-    T2<T> *__restrict__ aOut, T *__restrict__ alphaOut, uint32_t *__restrict__ flags);
+    T2<T> *__restrict__ aOut, T *__restrict__ alphaOut, uint32_t *__restrict__ flags,
+    const int32_t *__restrict__ perm, T2<T> *__restrict__ tx, T2<T> *__restrict__ tv);
 
 // accel_kernel! (pressure + viscosity + gravity + wall, and alpha) fused with
 // integrate_kernel! (semi-implicit Euler, implicit Brinkman drag).
@@ -604,7 +605,9 @@ __global__ void __launch_bounds__(kBlock)
                       const T2<T> *__restrict__ prho, const T *__restrict__ rho,
                       const T *__restrict__ theta, T2<T> *__restrict__ posOut,
                       T2<T> *__restrict__ velOut, T2<T> *__restrict__ aOut,
-                      T *__restrict__ alphaOut, uint32_t *__restrict__ flags)
+                      T *__restrict__ alphaOut, uint32_t *__restrict__ flags,
+                      const int32_t *__restrict__ perm, T2<T> *__restrict__ tx,
+                      T2<T> *__restrict__ tv)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
@@ -614,7 +617,8 @@ __global__ void __launch_bounds__(kBlock)
     const T2<T> vi = vel[i];
     T ax, ay;
     accel_sum<T, AV>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
-    accel_integrate_finish<T>(I, b, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags);
+    accel_integrate_finish<T>(I, b, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags,
+                              perm, tx, tv);
 }
 
 // Gravity, wall, alpha and the integrator of one particle, after its pair sum.
@@ -622,9 +626,17 @@ template <typename T, typename IT>
 __device__ __forceinline__ void accel_integrate_finish(
     const IT &I, int b, int64_t i, const T2<T> &xi, const T2<T> &vi, T ax, T ay,
     const T *__restrict__ theta, T2<T> *__restrict__ posOut, T2<T> *__restrict__ velOut,
-    T2<T> *__restrict__ aOut, T *__restrict__ alphaOut, uint32_t *__restrict__ flags)
+    T2<T> *__restrict__ aOut, T *__restrict__ alphaOut, uint32_t *__restrict__ flags,
+    const int32_t *__restrict__ perm, T2<T> *__restrict__ tx, T2<T> *__restrict__ tv)
 {
     const Phys<T> &p = I.p;
+    if (tx) {
+        // _tape_store! (src/driver.jl:73-77) of the pre-step state, in
+        // particle-id order
+        const int32_t id = perm[i];
+        tx[id] = xi;
+        tv[id] = vi;
+    }
     const T al = interp_alpha_value<T>(theta + I.toff, xi.x, xi.y, p);
     ax += p.gx + wall_accel<T>(xi.x, p.Lx, p.kw);
     ay += p.gy + wall_accel<T>(xi.y, p.Ly, p.kw);
@@ -640,19 +652,6 @@ __device__ __forceinline__ void accel_integrate_finish(
     posOut[i] = mk2<T>(x1, x2);
     if (!(isfinite(x1) && isfinite(x2) && isfinite(v1) && isfinite(v2)))
         atomicOr(flags + b, FLAG_NONFINITE);
-}
-
-// Tape slot in particle-id order (_tape_store!, src/driver.jl:73-77).
-template <typename T>
-__global__ void k_tape_store(int64_t N, const int32_t *__restrict__ perm,
-                             const T2<T> *__restrict__ pos, const T2<T> *__restrict__ vel,
-                             T2<T> *__restrict__ tx, T2<T> *__restrict__ tv)
-{
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= N) return;
-    const int32_t id = perm[i];
-    tx[id] = pos[i];
-    tv[id] = vel[i];
 }
 
 // _tape_load! into cell order: slot t takes particle perm[t]; when srcInv is
