@@ -594,7 +594,30 @@ template <typename T> class Sys final : public StateI {
                  T2<T> *ex1N = nullptr)
     {
         const int check = age != INT64_MAX ? 1 : 0;
-        if (N_ > 0) {
+        if (sizeof(T) == 4 && N_ > 0 && B == 1 && N_ <= kRebuildSmallMaxN &&
+            ncell <= kRebuildSmallMaxCells) {
+            // small single FP32 state: the cell list in one launch (the
+            // reference's GPU optimisation set-up, 1500 particles, runs 12%
+            // faster; in FP64 the one block's double-precision cell
+            // coordinates cost more than the launches saved)
+            const int nxt = 1 - cur;
+            const size_t smem = sizeof(int32_t) * (size_t)(2 * ncell + 1 + 3 * N_);
+            static bool attr = false;
+            if (!attr) {
+                SPH_CK(cudaFuncSetAttribute(k_rebuild_small<T>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)(sizeof(int32_t) * (2 * kRebuildSmallMaxCells + 1 +
+                                                                     3 * kRebuildSmallMaxN))));
+                attr = true;
+            }
+            rt_before_launch(K_RANK);
+            k_rebuild_small<T><<<1, kRebuildSmallThreads, smem, rt_stream()>>>(
+                (int)N_, (int)ncell, hinst[0], check, pos[cur].p, vel[cur].p, pos[nxt].p,
+                vel[nxt].p, xref.p, perm.p, invperm.p, cellStart.p, ex0, ex0N, ex1, ex1N, flags.p);
+            rt_after_launch(K_RANK);
+            cur = nxt;
+            build_masks();
+        } else if (N_ > 0) {
             counts.zero();
             auto ka = B > 1 ? &k_assign<T, true> : &k_assign<T, false>;
             SPH_LAUNCH(K_ASSIGN, ka, N_, N_, pos[cur].p, xref.p, check, hinst[0], dinst.p, pinst.p,
@@ -606,18 +629,24 @@ template <typename T> class Sys final : public StateI {
                        bucketId.p, pos[cur].p, vel[cur].p, pos[nxt].p, vel[nxt].p, xref.p, perm.p,
                        invperm.p, ex0, ex0N, ex1, ex1N);
             cur = nxt;
-            if (const int G = group_lanes()) {
-                auto kn = G == 32 ? &k_nl_build_coop<T, 32> : &k_nl_build_coop<T, 16>;
-                SPH_LAUNCH_COOP(K_NLBUILD, G, kn, N_, N_, hinst[0], pos[cur].p, cellStart.p,
-                                center.p, masks.p, nbcount.p, flags.p);
-            } else {
-                auto kn = B > 1 ? &k_nl_build<T, true> : &k_nl_build<T, false>;
-                SPH_LAUNCH_TUNED(K_NLBUILD, B > 1, kn, N_, N_, hinst[0], dinst.p, pinst.p,
-                                 pos[cur].p, cellStart.p, center.p, masks.p, nbcount.p, flags.p);
-            }
+            build_masks();
         }
         age = 0;
         cellsOnlyLatest = false;
+    }
+
+    // _nl_build! on the freshly sorted particles
+    void build_masks()
+    {
+        if (const int G = group_lanes()) {
+            auto kn = G == 32 ? &k_nl_build_coop<T, 32> : &k_nl_build_coop<T, 16>;
+            SPH_LAUNCH_COOP(K_NLBUILD, G, kn, N_, N_, hinst[0], pos[cur].p, cellStart.p,
+                            center.p, masks.p, nbcount.p, flags.p);
+        } else {
+            auto kn = B > 1 ? &k_nl_build<T, true> : &k_nl_build<T, false>;
+            SPH_LAUNCH_TUNED(K_NLBUILD, B > 1, kn, N_, N_, hinst[0], dinst.p, pinst.p,
+                             pos[cur].p, cellStart.p, center.p, masks.p, nbcount.p, flags.p);
+        }
     }
 
     void build_neighbors() override

@@ -216,6 +216,116 @@ __global__ void k_rank_permute(int64_t N, const int32_t *__restrict__ cellTmp,
     if (ex1) ex1N[dst] = ex1[src];
 }
 
+// The whole cell-list rebuild of a small single FP32 state in one block: cells
+// and the displacement check (k_assign), the exclusive scan (k_scan_*), the
+// bucket and the in-cell rank by particle id (k_bucket, k_rank_permute), with
+// the histogram, scan and buckets in shared memory. Same arithmetic and the
+// same deterministic order as the multi-launch path; it saves four launches
+// per rebuild when the state is too small to keep the GPU busy anyway.
+// Dynamic shared memory: 4 * (ncell + (ncell + 1) + 3 N) bytes.
+constexpr int kRebuildSmallThreads = 1024;
+constexpr int64_t kRebuildSmallMaxN = 4096;
+constexpr int64_t kRebuildSmallMaxCells = 8192;
+
+template <typename T>
+__global__ void __launch_bounds__(kRebuildSmallThreads)
+    k_rebuild_small(int N, int ncell, const Inst<T> I, int check, const T2<T> *__restrict__ pos,
+                    const T2<T> *__restrict__ vel, T2<T> *__restrict__ posN,
+                    T2<T> *__restrict__ velN, T2<T> *__restrict__ xref, int32_t *__restrict__ perm,
+                    int32_t *__restrict__ invperm, int32_t *__restrict__ cellStart,
+                    const T2<T> *__restrict__ ex0, T2<T> *__restrict__ ex0N,
+                    const T2<T> *__restrict__ ex1, T2<T> *__restrict__ ex1N,
+                    uint32_t *__restrict__ flags)
+{
+    extern __shared__ int32_t sm[];
+    int32_t *cursor = sm;                  // ncell: counts, then running cursors
+    int32_t *starts = cursor + ncell;      // ncell + 1
+    int32_t *cellOf = starts + ncell + 1;  // N
+    int32_t *bucketSrc = cellOf + N;       // N
+    int32_t *bucketId = bucketSrc + N;     // N
+    __shared__ int32_t part[kRebuildSmallThreads / 32 + 1];
+    const int t = (int)threadIdx.x, nt = (int)blockDim.x;
+    for (int c = t; c < ncell; c += nt) cursor[c] = 0;
+    __syncthreads();
+    // cells (x / cs as in cell_index) and the displacement check
+    bool moved = false;
+    for (int i = t; i < N; i += nt) {
+        const T2<T> x = pos[i];
+        if (check) {
+            const T2<T> xr = xref[i];
+            const T d2 = r2_exact<T>(sub_rn(x.x, xr.x), sub_rn(x.y, xr.y));
+            moved = moved || d2 > I.dmax2;
+        }
+        const int cx = cell_coord<T>(x.x / I.cs, I.nx);
+        const int cy = cell_coord<T>(x.y / I.cs, I.ny);
+        const int c = I.coff + (cx - 1) + (cy - 1) * I.nx;
+        cellOf[i] = c;
+        atomicAdd(&cursor[c], 1);
+    }
+    if (__syncthreads_or(moved) && t == 0) atomicOr(flags, FLAG_DISPLACEMENT);
+    // exclusive scan of the counts: each thread sums a contiguous chunk
+    const int chunk = (ncell + nt - 1) / nt;
+    const int c0 = t * chunk, c1 = c0 + chunk < ncell ? c0 + chunk : ncell;
+    int32_t sum = 0;
+    for (int c = c0; c < c1; ++c) sum += cursor[c];
+    int32_t x = sum;
+    const int lane = t & 31, warp = t >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) part[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = nt >> 5;
+        int32_t w = lane < nw ? part[lane] : 0, v = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += y;
+        }
+        if (lane < nw) part[lane] = v - w;
+    }
+    __syncthreads();
+    int32_t run = x - sum + part[warp];
+    for (int c = c0; c < c1; ++c) {
+        const int32_t n = cursor[c];
+        starts[c] = run;
+        cellStart[c] = run;
+        cursor[c] = run;
+        run += n;
+    }
+    if (t == 0) {
+        starts[ncell] = N;
+        cellStart[ncell] = N;
+    }
+    __syncthreads();
+    // buckets: every particle into its cell's range (arbitrary order inside)
+    for (int i = t; i < N; i += nt) {
+        const int p = atomicAdd(&cursor[cellOf[i]], 1);
+        bucketSrc[p] = i;
+        bucketId[p] = perm[i];
+    }
+    __syncthreads();
+    // in-cell rank by particle id, and the data into the new order
+    for (int s = t; s < N; s += nt) {
+        const int src = bucketSrc[s], id = bucketId[s], c = cellOf[src];
+        const int b = starts[c], e = starts[c + 1];
+        int rank = 0;
+        for (int k = b; k < e; ++k) rank += bucketId[k] < id ? 1 : 0;
+        const int dst = b + rank;
+        perm[dst] = id;
+        const T2<T> xs = pos[src];
+        posN[dst] = xs;
+        xref[dst] = xs;
+        velN[dst] = vel[src];
+        invperm[id] = dst;
+        if (ex0) ex0N[dst] = ex0[src];
+        if (ex1) ex1N[dst] = ex1[src];
+    }
+}
+
 // _nl_build! (src/neighbors.jl:192-245): the scan centre uses x * invcs as
 // the reference does; a neighbour is kept if r2min < r^2 < rc^2, in scan order,
 // at most maxnb of them (overflow sets the flag, like flags[1]).
