@@ -72,3 +72,27 @@ def test_small_maxnb_truncation_matches_oracle(lanes):
         assert K.relerr(g["gtheta"], r["gtheta"]) <= 1e-12
     finally:
         S.set_group_lanes(0)
+
+
+@pytest.mark.parametrize("lanes", [1, 32])
+def test_non_finite_particle_is_flagged_and_isolated(lanes):
+    """A particle with a NaN position raises the non-finite flag, never enters
+    another particle's neighbour rows (its r^2 fails every test), and leaves
+    the other particles exactly as a run without it."""
+    S.set_group_lanes(lanes)
+    try:
+        case = K.adjoint_case(seed=13)
+        p = S.SPHParams(**case["p"])
+        X0 = case["X0"].copy()
+        X0[:, 0] = np.nan
+        st = S.State(X0, case["V0"], p, interval=2)
+        with pytest.warns(RuntimeWarning, match="non-finite"):
+            S.simulate(st, case["theta"], p, 4)
+        assert st.last_flags & 4
+        ref = S.State(case["X0"][:, 1:], case["V0"][:, 1:], p, interval=2)
+        S.simulate(ref, case["theta"], p, 4)
+        X, V = (np.asarray(a) for a in st.get())
+        Xr, Vr = (np.asarray(a) for a in ref.get())
+        assert np.array_equal(X[:, 1:], Xr) and np.array_equal(V[:, 1:], Vr)
+    finally:
+        S.set_group_lanes(0)
