@@ -209,10 +209,16 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, const Inst
 }
 
 // Per-pair square root and reciprocal. FP64 keeps IEEE sqrt and division
-// (reference-exact); FP32 uses the hardware reciprocal square root, which is
-// within a few ulp (the FP32 path is checked against FP64 by tolerance).
+// (reference-exact); FP32 uses the PTX approximate square root (one
+// instruction, sqrt(+0) = +0, within a few ulp; the FP32 path is checked
+// against FP64 by tolerance).
 __device__ __forceinline__ double pair_sqrt(double r2) { return sqrt(r2); }
-__device__ __forceinline__ float pair_sqrt(float r2) { return r2 > 0.f ? r2 * rsqrtf(r2) : 0.f; }
+__device__ __forceinline__ float pair_sqrt(float r2)
+{
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(r2));
+    return r;
+}
 
 // clamp(unsafe_trunc(Int, floor(v)) + 2, 1, n) (src/neighbors.jl:38-42,217-218).
 // The float clamp keeps the conversion defined; no finite result changes.
