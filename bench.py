@@ -640,6 +640,31 @@ def run_ours(args):
                 kernels[k] = {"ms": round(a.value, 3), "launches": b.value}
             L.sph_profile_enable(LB.KERNEL_ID[k], 0)
 
+    # Whole-solve roofline: algorithmic HBM bytes of every executed pass (the
+    # minimal dataflow's compulsory traffic, s = sizeof T): forward step 14s
+    # (density 4s + accel/integrate 10s), reverse step 48s (tape read 4s,
+    # density 4s, accel/drag 15s, pass 1 16s, pass 2 9s), the full tape's
+    # write 4s per step, a neighbour rebuild 4s + 12; snapshot copies are not
+    # counted. Rebuilds per solve are the build launches of the breakdown solve
+    # when it ran, else one per `interval` executed steps.
+    fwd_steps = args.nsteps + rec
+    rebuilds = (kernels["nl_build"]["launches"] if "nl_build" in kernels
+                else (fwd_steps + args.nsteps) // max(interval, 1))
+    solve_bytes = N * (14 * esz * fwd_steps + 48 * esz * args.nsteps
+                       + (4 * esz * args.nsteps if args.snapshots == 0 else 0)
+                       + (4 * esz + 12) * rebuilds)
+    solve_gbs = solve_bytes / (ms / args.steps / 1000.0) / 1e9  # per GPU
+    solve_roof = {"bound": "hbm", "achieved": solve_gbs, "peak": hbm, "unit": "GB/s",
+                  "frac": solve_gbs / hbm, "bytes_per_solve": solve_bytes,
+                  "forward_steps": fwd_steps, "reverse_steps": args.nsteps,
+                  "rebuilds": rebuilds}
+    # the same per pass, from the breakdown solve's event-timed launches
+    pass_roof = {}
+    for k, words in ALGO_WORDS.items():
+        if k in kernels and kernels[k]["ms"] > 0:
+            gbs = words * esz * N * kernels[k]["launches"] / (kernels[k]["ms"] / 1000.0) / 1e9
+            pass_roof[k] = {"achieved": round(gbs, 1), "frac": round(gbs / hbm, 4)}
+
     # the same solve in FP64 on the GPU (the FP64 oracle run of the workload):
     # relative difference of the FP32 results, max |a - b| / max |b|
     fp64 = None
@@ -730,6 +755,7 @@ def run_ours(args):
                 "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
                 "data": "synthetic", "config": cfg, "roofline": roof, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+                "solve_roofline": solve_roof, "pass_rooflines": pass_roof,
                 "recomputed_forward_steps_per_solve": rec,
                 "objective_J": J.value, "kernels_one_solve": kernels,
                 "block_sizes": blocks, "fp64_check": fp64, "graph": graph is not None,

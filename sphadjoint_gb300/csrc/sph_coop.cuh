@@ -12,8 +12,13 @@
 // memory, and one lane per running sum adds them in candidate order, so
 // every sum sees exactly the operations and the order of the serial loop:
 // results are bit-identical to the thread-per-particle kernels (and, in the
-// FP64 build, to the reference's). Particles whose rows spill past 64 slots
-// take the serial path on the group's first lane.
+// FP64 build, to the reference's). A particle whose rows spill past 64 slots
+// (a compressed region: the small dam break has up to ~130 of them while its
+// front runs along the floor) has no masks; its group scans the rows, keeps
+// the reference's row in slot order in shared memory and deals that list out
+// the same way (the serial path on one lane, used before, made those steps
+// 6-10x slower). Only a row limit maxnb above kSpillList falls back to the
+// serial walk on the group's first lane.
 #pragma once
 
 #include "sph_kernels.cuh"
@@ -21,6 +26,7 @@
 namespace sphgb {
 
 constexpr int kCoopBlock = 128;
+constexpr int kSpillList = 64; // neighbour list of a spilled particle, in shared memory
 
 // Position of the r-th (0-based) set bit of m; requires r < popc(m).
 __device__ __forceinline__ int select_bit(uint32_t m, int r)
@@ -63,15 +69,24 @@ template <int G> struct Group {
     }
 };
 
-// The candidates of a non-spilled particle: the set bits of its six words
-// (row r = words 2r, 2r+1), numbered 0..total-1 in slot order.
+// The candidates of a particle, numbered 0..total-1 in slot order: the set
+// bits of its six words (row r = words 2r, 2r+1), or for a spilled particle
+// the list spill_list built.
 template <typename T> struct Cands {
     uint32_t wd[6];
     int bs[6];  // slot of bit 0 of each word
     int pre[7]; // candidates before each word
+    const int32_t *lst; // spilled particle: its neighbour slots (shared memory)
+    int nl;
+    __device__ __forceinline__ void init_list(const int32_t *l, int n)
+    {
+        lst = l;
+        nl = n;
+    }
     __device__ __forceinline__ void init(const NLView<T> &v, const Inst<T> &I, int64_t i,
                                          uint32_t cc, const uint32_t *__restrict__ mk)
     {
+        lst = nullptr;
         const int cx = (int)(cc & 0xffffu);
         const int cy = (int)((cc >> 16) & 0x7fffu);
         const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
@@ -88,10 +103,16 @@ template <typename T> struct Cands {
 #pragma unroll
         for (int w = 0; w < 6; ++w) pre[w + 1] = pre[w] + __popc(wd[w]);
     }
-    __device__ __forceinline__ int total() const { return pre[6]; }
-    // slot of candidate k < total(); w, bit: its word and bit
+    __device__ __forceinline__ int total() const { return lst ? nl : pre[6]; }
+    // slot of candidate k < total(); w, bit: its word and bit (w = -1 for a
+    // listed candidate: a spilled particle has no in-support words)
     __device__ __forceinline__ int slot(int k, int &w, int &bit) const
     {
+        if (lst) {
+            w = -1;
+            bit = 0;
+            return lst[k];
+        }
         uint32_t word = wd[0];
         int base = bs[0], rem = k;
         w = 0;
@@ -107,6 +128,49 @@ template <typename T> struct Cands {
         return base + bit;
     }
 };
+
+// The neighbour row of a spilled particle as the generic walk of
+// for_each_neighbor visits it: r2min < r^2 < rc^2 on the rebuild positions,
+// rows ddy = -1..1, slot order, at most maxnb (<= kSpillList) entries. Each
+// round tests G consecutive slots; a ballot gives the kept ones, which are
+// written to lst at their rank. Returns the count (the same on every lane).
+template <typename T, int G>
+__device__ __forceinline__ int spill_list(const Group<G> &g, const NLView<T> &v,
+                                          const Inst<T> &I, int64_t i, uint32_t cc,
+                                          int32_t *__restrict__ lst)
+{
+    const int cx = (int)(cc & 0xffffu);
+    const int cy = (int)((cc >> 16) & 0x7fffu);
+    const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
+    const int jx1 = cx + 1 < I.nx ? cx + 1 : I.nx;
+    const T2<T> xr = v.xref[i];
+    const int maxnb = I.maxnb;
+    int cnt = 0;
+#pragma unroll 1
+    for (int r = 0; r < 3; ++r) {
+        const int jy = cy + r - 1;
+        if (jy < 1 || jy > I.ny) continue;
+        const int row = I.coff + (jy - 1) * I.nx;
+        const int b = v.cellStart[row + jx0 - 1];
+        const int e = v.cellStart[row + jx1];
+        for (int base = b; base < e && cnt < maxnb; base += G) {
+            const int j = base + g.gl;
+            bool pass = false;
+            if (j < e) {
+                const T2<T> xj = v.xref[j];
+                const T r2 = r2_exact<T>(sub_rn(xr.x, xj.x), sub_rn(xr.y, xj.y));
+                pass = I.r2min < r2 && r2 < I.rc2;
+            }
+            uint32_t kept = g.ballot(pass);
+            const int room = maxnb - cnt;
+            if (__popc(kept) > room) kept &= (1u << select_bit(kept, room)) - 1u;
+            if ((kept >> g.gl) & 1u) lst[cnt + __popc(kept & ((1u << g.gl) - 1u))] = j;
+            cnt += __popc(kept);
+        }
+    }
+    g.sync();
+    return cnt;
+}
 
 // _nl_build! (src/neighbors.jl:192-245) with the row scan spread over the
 // group: each round tests G consecutive slots, a ballot gives the passing
@@ -184,6 +248,7 @@ __global__ void __launch_bounds__(kCoopBlock)
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][G];
     __shared__ uint32_t tws[NG][6];
+    __shared__ int32_t lst[NG][kSpillList];
     const Group<G> g;
     const int64_t i = (int64_t)blockIdx.x * NG + g.gi;
     if (i >= v.N) return;
@@ -191,12 +256,13 @@ __global__ void __launch_bounds__(kCoopBlock)
     const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, A = I.p.A;
     const T2<T> xi = v.pos[i];
     const uint32_t cc = v.center[i];
-    if (cc >> 31) {
+    if ((cc >> 31) && I.maxnb > kSpillList) {
         if (g.gl == 0) density_finish<T>(I, i, density_spill_sum<T>(v, I, i, xi, tmaskOut), rho, prho);
         return;
     }
     Cands<T> cd;
-    cd.init(v, I, i, cc, v.masks);
+    if (cc >> 31) cd.init_list(lst[g.gi], spill_list<T, G>(g, v, I, i, cc, lst[g.gi]));
+    else cd.init(v, I, i, cc, v.masks);
     const int K = cd.total();
     if (g.gl < 6) tws[g.gi][g.gl] = 0u;
     g.sync();
@@ -214,7 +280,7 @@ __global__ void __launch_bounds__(kCoopBlock)
             if (r2 < r2max) {
                 in = true;
                 c = density_pair<T>(r2, invh, m, A);
-                atomicOr(&tws[g.gi][w], 1u << bit);
+                if (w >= 0) atomicOr(&tws[g.gi][w], 1u << bit);
             }
         }
         buf[g.gi][g.gl] = c;
@@ -233,10 +299,23 @@ __global__ void __launch_bounds__(kCoopBlock)
 
 // Pressure + viscosity pair sum of one particle by its group; lane 0 returns
 // (ax, ay).
+// The candidates of particle i for a pass after the density pass: this step's
+// in-support words, or for a spilled particle its listed row.
+template <typename T, int G>
+__device__ __forceinline__ Cands<T> pass_cands(const Group<G> &g, const NLView<T> &v,
+                                               const Inst<T> &I, int64_t i, uint32_t cc,
+                                               int32_t *__restrict__ lst)
+{
+    Cands<T> cd;
+    if (cc >> 31) cd.init_list(lst, spill_list<T, G>(g, v, I, i, cc, lst));
+    else cd.init(v, I, i, cc, v.tmask ? v.tmask : v.masks);
+    return cd;
+}
+
 template <typename T, int G, int NG>
 __device__ __forceinline__ void accel_sum_coop(const Group<G> &g, T (*buf)[4][G],
                                                const NLView<T> &v, const Inst<T> &I, int64_t i,
-                                               uint32_t cc, const T2<T> *__restrict__ vel,
+                                               const Cands<T> &cd, const T2<T> *__restrict__ vel,
                                                const T2<T> *__restrict__ prho,
                                                const T *__restrict__ rho, const T2<T> &xi,
                                                const T2<T> &vi, T &ax, T &ay)
@@ -246,8 +325,6 @@ __device__ __forceinline__ void accel_sum_coop(const Group<G> &g, T (*buf)[4][G]
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
     const T rhoi = vc.kind == 1 ? rho[i] : (T)0;
-    Cands<T> cd;
-    cd.init(v, I, i, cc, v.tmask ? v.tmask : v.masks);
     const int K = cd.total();
     T acc = (T)0; // lane 0: ax, lane 1: ay
     for (int base = 0; base < K; base += G) {
@@ -303,6 +380,7 @@ __global__ void __launch_bounds__(kCoopBlock)
 {
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][4][G];
+    __shared__ int32_t lst[NG][kSpillList];
     const Group<G> g;
     const int64_t i = (int64_t)blockIdx.x * NG + g.gi;
     if (i >= v.N) return;
@@ -311,11 +389,12 @@ __global__ void __launch_bounds__(kCoopBlock)
     const T2<T> vi = vel[i];
     const uint32_t cc = v.center[i];
     T ax, ay;
-    if (cc >> 31) {
+    if ((cc >> 31) && I.maxnb > kSpillList) {
         if (g.gl != 0) return;
         accel_sum<T, true>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
     } else {
-        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, rho, xi, vi, ax, ay);
+        const Cands<T> cd = pass_cands<T, G>(g, v, I, i, cc, lst[g.gi]);
+        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cd, vel, prho, rho, xi, vi, ax, ay);
         if (g.gl != 0) return;
     }
     accel_integrate_finish<T>(I, 0, i, xi, vi, ax, ay, theta, posOut, velOut, aOut, alphaOut, flags,
@@ -335,6 +414,7 @@ __global__ void __launch_bounds__(kCoopBlock)
 {
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][4][G];
+    __shared__ int32_t lst[NG][kSpillList];
     const Group<G> g;
     const int64_t i = (int64_t)blockIdx.x * NG + g.gi;
     if (i >= v.N) return;
@@ -343,11 +423,12 @@ __global__ void __launch_bounds__(kCoopBlock)
     const T2<T> vi = vel[i];
     const uint32_t cc = v.center[i];
     T ax, ay;
-    if (cc >> 31) {
+    if ((cc >> 31) && I.maxnb > kSpillList) {
         if (g.gl != 0) return;
         accel_sum<T, true>(v, I, vel, prho, rho, i, xi, vi, ax, ay);
     } else {
-        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cc, vel, prho, rho, xi, vi, ax, ay);
+        const Cands<T> cd = pass_cands<T, G>(g, v, I, i, cc, lst[g.gi]);
+        accel_sum_coop<T, G, NG>(g, buf, v, I, i, cd, vel, prho, rho, xi, vi, ax, ay);
         if (g.gl != 0) return;
     }
     const int e = drag_adj_finish<T>(I, i, xi, vi, ax, ay, theta, gX, gV, abar, galpha);
@@ -366,6 +447,7 @@ __global__ void __launch_bounds__(kCoopBlock)
 {
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][9][G]; // eight term slots and a row of zeros
+    __shared__ int32_t lst[NG][kSpillList];
     const Group<G> g;
     const int64_t i = (int64_t)blockIdx.x * NG + g.gi;
     if (i >= v.N) return;
@@ -376,7 +458,7 @@ __global__ void __launch_bounds__(kCoopBlock)
     const T2<T> pi = prho[i];
     const uint32_t cc = v.center[i];
     T gx, gy, gvx, gvy, grh, sumS;
-    if (cc >> 31) {
+    if ((cc >> 31) && I.maxnb > kSpillList) {
         if (g.gl != 0) return;
         pass1_sum<T, true>(v, I, i, vel, prho, rho, abar, xi, vi, ab, pi, gx, gy, gvx, gvy, grh,
                            sumS);
@@ -385,8 +467,7 @@ __global__ void __launch_bounds__(kCoopBlock)
         const Visc<T> vc = visc_of<T>(I);
         const T pti = pi.x, iri = pi.y;
         const T rhoi = vc.kind == 1 ? rho[i] : (T)0;
-        Cands<T> cd;
-        cd.init(v, I, i, cc, v.tmask ? v.tmask : v.masks);
+        const Cands<T> cd = pass_cands<T, G>(g, v, I, i, cc, lst[g.gi]);
         const int K = cd.total();
         // term slots: 0 gx-, 1 gx+, 2 gy-, 3 gy+, 4 gvx+, 5 gvy+, 6 grho-, 7 S+,
         // 8 zeros. Every running sum takes "minus one slot, plus one slot" per
@@ -461,6 +542,7 @@ __global__ void __launch_bounds__(kCoopBlock)
 {
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][2][G];
+    __shared__ int32_t lst[NG][kSpillList];
     const Group<G> g;
     const int64_t i = (int64_t)blockIdx.x * NG + g.gi;
     if (i >= v.N) return;
@@ -470,7 +552,7 @@ __global__ void __launch_bounds__(kCoopBlock)
     const T gri = grho[i];
     const uint32_t cc = v.center[i];
     T gx = (T)0, gy = (T)0;
-    if (cc >> 31) {
+    if ((cc >> 31) && I.maxnb > kSpillList) {
         if (g.gl != 0) return;
         for_each_neighbor<T>(v, I, i, [&](int j) {
             const T2<T> xj = v.pos[j];
@@ -484,8 +566,7 @@ __global__ void __launch_bounds__(kCoopBlock)
             }
         });
     } else {
-        Cands<T> cd;
-        cd.init(v, I, i, cc, v.tmask ? v.tmask : v.masks);
+        const Cands<T> cd = pass_cands<T, G>(g, v, I, i, cc, lst[g.gi]);
         const int K = cd.total();
         T acc = (T)0;
         for (int base = 0; base < K; base += G) {

@@ -36,16 +36,21 @@ def dense_case():
                 cX=rng.standard_normal(X0.shape), cV=rng.standard_normal(X0.shape))
 
 
+# name: (case, steps, rebuild interval, maxnb). "dense": spilled particles,
+# whose groups list their rows in shared memory, and maxnb truncation;
+# "dense-maxnb96": a row limit above the shared list, where spilled particles
+# take the serial walk on one lane.
 CASES = {
-    "adjoint": (lambda: K.adjoint_case(seed=5), 12, 4),
-    "dambreak": (lambda: K.dambreak_case(theta_seed=4, jitter=0.05), 40, 4),
-    "dense": (dense_case, 8, 2),
+    "adjoint": (lambda: K.adjoint_case(seed=5), 12, 4, 64),
+    "dambreak": (lambda: K.dambreak_case(theta_seed=4, jitter=0.05), 40, 4, 64),
+    "dense": (dense_case, 8, 2, 64),
+    "dense-maxnb96": (dense_case, 6, 2, 96),
 }
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_fp64_bit_identical_across_lane_settings(lanes, name):
-    make, n, interval = CASES[name]
+    make, n, interval, maxnb = CASES[name]
     case = make()
     if "cX" not in case:
         rng = np.random.default_rng(3)
@@ -55,10 +60,10 @@ def test_fp64_bit_identical_across_lane_settings(lanes, name):
     out = {}
     for g in (1, 16, 32):
         lanes(g)
-        out[g] = run_gpu(case, n, seeds=seeds, interval=interval)
+        out[g] = run_gpu(case, n, seeds=seeds, interval=interval, maxnb=maxnb)
         nb, cnt = out[g]["state"].neighbors()
         out[g]["nb"], out[g]["cnt"] = nb, cnt
-    r = run_oracle(case, n, seeds=seeds, interval=interval)
+    r = run_oracle(case, n, seeds=seeds, interval=interval, maxnb=maxnb)
     for g in (16, 32):
         for k in ("X", "V", "gX", "gV", "gtheta", "nb", "cnt"):
             assert np.array_equal(out[g][k], out[1][k]), (g, k)
