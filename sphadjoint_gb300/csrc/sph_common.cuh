@@ -41,6 +41,22 @@ template <typename T> __device__ __forceinline__ T r2_exact(T dx, T dy)
     return add_rn(mul_rn(dx, dx), mul_rn(dy, dy));
 }
 
+// Position of the r-th (0-based) set bit of m; requires r < popc(m).
+__device__ __forceinline__ int select_bit(uint32_t m, int r)
+{
+    int pos = 0;
+    int c = __popc(m & 0xffffu);
+    if (r >= c) { r -= c; m >>= 16; pos += 16; }
+    c = __popc(m & 0xffu);
+    if (r >= c) { r -= c; m >>= 8; pos += 8; }
+    c = __popc(m & 0xfu);
+    if (r >= c) { r -= c; m >>= 4; pos += 4; }
+    c = __popc(m & 0x3u);
+    if (r >= c) { r -= c; m >>= 2; pos += 2; }
+    if (r >= (int)(m & 1u)) pos += 1;
+    return pos;
+}
+
 // SPHParams{T} (src/params.jl:58-72) plus the constants each reference kernel
 // forms from it, formed on the host in T with the same association:
 //   A = T(7)/(T(4)*T(pi)*h^2), invh = 1/h, r2max = T(4)*h*h,

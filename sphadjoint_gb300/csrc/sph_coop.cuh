@@ -28,22 +28,6 @@ namespace sphgb {
 constexpr int kCoopBlock = 128;
 constexpr int kSpillList = 64; // neighbour list of a spilled particle, in shared memory
 
-// Position of the r-th (0-based) set bit of m; requires r < popc(m).
-__device__ __forceinline__ int select_bit(uint32_t m, int r)
-{
-    int pos = 0;
-    int c = __popc(m & 0xffffu);
-    if (r >= c) { r -= c; m >>= 16; pos += 16; }
-    c = __popc(m & 0xffu);
-    if (r >= c) { r -= c; m >>= 8; pos += 8; }
-    c = __popc(m & 0xfu);
-    if (r >= c) { r -= c; m >>= 4; pos += 4; }
-    c = __popc(m & 0x3u);
-    if (r >= c) { r -= c; m >>= 2; pos += 2; }
-    if (r >= (int)(m & 1u)) pos += 1;
-    return pos;
-}
-
 // Lanes of one group inside its warp.
 template <int G> struct Group {
     int gl;         // lane within the group
