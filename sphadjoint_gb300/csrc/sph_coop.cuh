@@ -2,7 +2,8 @@
 // single states too small to fill the GPU one thread per particle (a 2072-
 // particle dam break runs 17 blocks; in FP64 those 17 SMs are bound by the
 // double-precision pipe while 135 SMs idle). With 16-lane groups the same
-// state runs 518 blocks and its pass-1 kernel keeps the FP64 pipe ~80% busy.
+// state runs 259 blocks of 128 threads on every SM and its pass-1 kernel
+// keeps the FP64 pipe ~70% busy.
 //
 // A group of G lanes (16 or 32) owns one particle. The particle's candidate
 // neighbours (the set bits of its six mask words, in slot order = the
@@ -14,7 +15,7 @@
 // results are bit-identical to the thread-per-particle kernels (and, in the
 // FP64 build, to the reference's). A particle whose rows spill past 64 slots
 // (a compressed region: the small dam break has up to ~130 of them while its
-// front runs along the floor) has no masks; its group scans the rows, keeps
+// front runs along the floor) has masks for the first 64 slots only; its group scans the rows, keeps
 // the reference's row in slot order in shared memory and deals that list out
 // the same way (the serial path on one lane, used before, made those steps
 // 6-10x slower). Only a row limit maxnb above kSpillList falls back to the
