@@ -60,4 +60,7 @@ def test_gpu_arm_line():
     assert s["bytes_per_solve"] > 0 and s["achieved"] > 0
     assert d["gpu_launches"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
-    assert "sm_mhz" in d["clocks"] and "reasons" in d["clocks"]
+    # nvidia-smi samples every 200 ms: a timed region this short may see none
+    assert "clocks" in d
+    if d["clocks"] is not None:
+        assert "sm_mhz" in d["clocks"] and "reasons" in d["clocks"]
