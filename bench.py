@@ -123,7 +123,7 @@ def dense_workload(side=2896, ntheta=512, seed=5):
     return p, X0, np.zeros_like(X0), theta, cfg
 
 
-def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3):
+def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3, snapshots=0):
     """64 independent dam breaks: N log-uniform in [1k, 64k], aspect (height /
     width of the water block) uniform in [0.3, 1.0], each with its own seeded,
     box-smoothed 64 x 64 theta; dx = 1e-3, tank 2W x 1.25 max(W, H)."""
@@ -149,9 +149,10 @@ def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3):
         theta = sum(pad[i:i + ntheta, j:j + ntheta] for i in range(5) for j in range(5)) / 25.0
         inst.append((p, X0, np.zeros_like(X0), theta))
     cfg = {"workload": f"batched: {B} dam breaks, N log-uniform in [1k, 64k], aspect in [0.3, 1], "
-                       f"own {ntheta}x{ntheta} theta each, {nsteps} steps FP32, full tape",
+                       f"own {ntheta}x{ntheta} theta each, {nsteps} steps FP32, "
+                       + ("full tape" if snapshots == 0 else f"{snapshots} checkpoint slots"),
            "instances": B, "particles": int(sum(x[1].shape[1] for x in inst)),
-           "time_steps": nsteps, "theta": [ntheta, ntheta], "dx": dx,
+           "time_steps": nsteps, "snapshots": snapshots, "theta": [ntheta, ntheta], "dx": dx,
            "skin": 0.2, "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half"}
     return inst, cfg
 
@@ -167,7 +168,7 @@ def run_batched(args):
     L = S.load()
     stream = torch.cuda.Stream()
     LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
-    inst, cfg = batched_workload(args.instances, args.nsteps)
+    inst, cfg = batched_workload(args.instances, args.nsteps, snapshots=args.snapshots)
     ps = [S.SPHParams(**p, dtype=args.dtype) for p, _, _, _ in inst]
     ntot = sum(x[1].shape[1] for x in inst)
     flags = C.c_uint32()
@@ -782,8 +783,11 @@ def main():
                     help="physics: the reference's (linear EOS, Morris viscosity) or Tait + "
                          "artificial viscosity")
     ap.add_argument("--side", type=int, default=1024, help="lattice side (particles = side^2)")
-    ap.add_argument("--nsteps", type=int, default=1000)
-    ap.add_argument("--snapshots", type=int, default=32)
+    ap.add_argument("--nsteps", type=int, default=None,
+                    help="time steps per solve (single: 1000; batched: 2000; small and dense "
+                         "fix their own)")
+    ap.add_argument("--snapshots", type=int, default=None,
+                    help="checkpoint slots, 0 = full tape (single: 32; batched: full tape)")
     ap.add_argument("--ntheta", type=int, default=256)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
     ap.add_argument("--kernel", default="pass1", choices=sorted(ALGO_WORDS))
@@ -806,6 +810,11 @@ def main():
     ap.add_argument("--autotune", type=int, default=1,
                     help="measure per-kernel block sizes on the workload before timing")
     args = ap.parse_args()
+    batched = args.workload == "batched"
+    if args.nsteps is None:
+        args.nsteps = 2000 if batched else 1000
+    if args.snapshots is None:
+        args.snapshots = 0 if batched else 32
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
