@@ -36,6 +36,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# steps of the short solves that choose the block sizes inside the solve
+TUNE_STEPS = 32
+
 # algorithmic HBM bytes per particle per launch (compulsory traffic of the
 # minimal dataflow, s = sizeof(T)): read/write sets of each fused pass
 ALGO_WORDS = {
@@ -180,16 +183,21 @@ def run_batched(args):
     ws = S.BatchWorkspace(bt)
     Jb = (C.c_double * len(inst))()
 
+    def solve_batch(nsteps=None, tp=None):
+        nsteps, tp = nsteps or args.nsteps, tp or tape
+        LB.check(L.sph_state_assign(bt.h, bt0.h))
+        tp.reset()
+        LB.check(L.sph_simulate(bt.h, th.h, None, nsteps, tp.h, C.byref(flags)))
+        LB.check(L.sph_batch_objective(ws.h, bt.h, 0, None, Jb))
+        LB.check(L.sph_backward_seeded(ws.h, tp.h, th.h, None, None, 0.2, 4, 64, C.byref(flags)))
+
     if args.autotune:
         b6 = (C.c_int32 * 6)()
         LB.check(L.sph_autotune(bt.h, th.h, 5, b6))
-
-    def solve_batch():
-        LB.check(L.sph_state_assign(bt.h, bt0.h))
-        tape.reset()
-        LB.check(L.sph_simulate(bt.h, th.h, None, args.nsteps, tape.h, C.byref(flags)))
-        LB.check(L.sph_batch_objective(ws.h, bt.h, 0, None, Jb))
-        LB.check(L.sph_backward_seeded(ws.h, tape.h, th.h, None, None, 0.2, 4, 64, C.byref(flags)))
+        tape_t = S.Tape(ntot, TUNE_STEPS, ps[0], snapshots=0)
+        solve_batch(TUNE_STEPS, tape_t)  # first use allocates
+        S.autotune_in_solve(bt, lambda: solve_batch(TUNE_STEPS, tape_t))
+        del tape_t
 
     def timed(fn, reps):
         for _ in range(args.warmup):
@@ -561,11 +569,24 @@ def run_ours(args):
 
     blocks = None
     if args.autotune:
-        # block sizes measured on this workload's initial state
+        # block sizes: the engine's autotune on this workload's initial state,
+        # then each kernel's fastest size inside short solves of the workload
         b6 = (C.c_int32 * 6)()
         LB.check(L.sph_autotune(st.h, th.h, 5, b6))
-        blocks = dict(zip(["nl_build", "density", "accel_integrate", "accel_drag", "pass1",
-                           "pass2"], list(b6)))
+        tape_t = S.Tape(N, TUNE_STEPS, p, snapshots=0)
+
+        def solve_short():
+            LB.check(L.sph_state_assign(st.h, st0.h))
+            tape_t.reset()
+            LB.check(L.sph_simulate(st.h, th.h, C.byref(pc), TUNE_STEPS, tape_t.h,
+                                    C.byref(flags)))
+            LB.check(L.sph_objective(ws.h, st.h, 0, None, C.byref(pc), C.byref(J)))
+            LB.check(L.sph_backward_seeded(ws.h, tape_t.h, th.h, C.byref(pc), None, 0.2,
+                                           interval, 64, C.byref(flags)))
+
+        solve_short()  # first use allocates
+        blocks = dict(zip(S.TUNED_KERNELS, S.autotune_in_solve(st, solve_short)))
+        del tape_t
     for _ in range(args.warmup):
         solve()
     torch.cuda.synchronize()

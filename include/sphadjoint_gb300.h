@@ -277,6 +277,14 @@ SPH_API int32_t sph_build_cells_noalloc(const void *X_dev, int64_t N, int32_t dt
    order. Runs on the state's own arrays and a temporary workspace; the state's
    positions and velocities are not changed. */
 SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_t *blocks);
+/* Set or read the six block sizes directly (same order; each 64, 128 or 256,
+   else SPH_ERR_ARG), for this state's precision and kind. A caller can time
+   the kernels inside its own solves with sph_profile_* and keep the fastest
+   per kernel (the Python mirror's autotune_in_solve does this): repeated
+   launches of one kernel, as sph_autotune times them, can favour a size that
+   is slower inside the solve's kernel sequence. */
+SPH_API int32_t sph_set_block_sizes(sph_state st, const int32_t *blocks);
+SPH_API int32_t sph_get_block_sizes(sph_state st, int32_t *blocks);
 
 /* Lanes per particle of the neighbour-list and pair-sum kernels (no
    counterpart in the reference), process-wide. 0 (default): by state size --

@@ -15,6 +15,8 @@ from .api import (  # noqa: F401
     State,
     Tape,
     backward,
+    TUNED_KERNELS,
+    autotune_in_solve,
     backward_seeded,
     capture,
     Graph,

@@ -97,6 +97,8 @@ _SIGS = {
     "sph_workspace_get": (_I32, [_P, _P, _P, _P]),
     "sph_state_assign": (_I32, [_P, _P]),
     "sph_autotune": (_I32, [_P, _P, _I32, _I32P]),
+    "sph_set_block_sizes": (_I32, [_P, _I32P]),
+    "sph_get_block_sizes": (_I32, [_P, _I32P]),
     "sph_set_group_lanes": (_I32, [_I32]),
     "sph_capture_begin": (_I32, []),
     "sph_capture_end": (_I32, [_PP]),

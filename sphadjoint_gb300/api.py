@@ -220,6 +220,18 @@ class State:
         L.check(self._L.sph_state_take_flags(self.h, C.byref(f)))
         return f.value
 
+    def set_block_sizes(self, blocks) -> None:
+        """Threads per block of the six tuned kernels (neighbour-list build,
+        density, accel, drag, pass 1, pass 2), each 64, 128 or 256, for every
+        object of this precision and kind (no counterpart in the reference)."""
+        b = (C.c_int32 * 6)(*[int(x) for x in blocks])
+        L.check(self._L.sph_set_block_sizes(self.h, b))
+
+    def block_sizes(self):
+        b = (C.c_int32 * 6)()
+        L.check(self._L.sph_get_block_sizes(self.h, b))
+        return list(b)
+
     def assign(self, src: "State") -> "State":
         """Make this state a device copy of src (same configuration): particles,
         order, neighbour structure and the neighbour-list age."""
@@ -402,6 +414,18 @@ class Batch:
         f = (C.c_uint32 * self.B)()
         L.check(self._L.sph_batch_take_flags(self.h, f))
         return list(f)
+
+    def set_block_sizes(self, blocks) -> None:
+        """Threads per block of the six tuned kernels (neighbour-list build,
+        density, accel, drag, pass 1, pass 2), each 64, 128 or 256, for every
+        object of this precision and kind (no counterpart in the reference)."""
+        b = (C.c_int32 * 6)(*[int(x) for x in blocks])
+        L.check(self._L.sph_set_block_sizes(self.h, b))
+
+    def block_sizes(self):
+        b = (C.c_int32 * 6)()
+        L.check(self._L.sph_get_block_sizes(self.h, b))
+        return list(b)
 
 
 class BatchField(DesignField):
@@ -703,6 +727,47 @@ def kinetic_energy_right_half(X, V, p: SPHParams):
 
 def launch_count() -> int:
     return int(L.load().sph_launch_count())
+
+
+TUNED_KERNELS = ("nl_build", "density", "accel_integrate", "accel_drag", "pass1", "pass2")
+
+
+def autotune_in_solve(state, solve, candidates=(64, 128, 256)):
+    """Choose the block size of each tuned kernel from its launches inside
+    real solves (no counterpart in the reference). solve() runs one short
+    forward+adjoint solve with ``state``'s precision and kind; it is called
+    once per candidate with every tuned kernel at that size, each kernel's
+    launches are timed with CUDA events, and each kernel keeps its fastest
+    size. Returns the chosen sizes (TUNED_KERNELS order).
+
+    Repeated launches of one kernel, as the engine's own autotune times them,
+    can favour a size that is slower inside the solve's kernel sequence (on
+    1M particles pass 2 runs 8% faster at 64 threads than at the 256 that
+    repeated launches pick)."""
+    lib = L.load()
+    ids = [L.KERNEL_ID[k] for k in TUNED_KERNELS]
+    best = [None] * 6
+    pick = [int(candidates[0])] * 6
+    try:
+        for c in candidates:
+            state.set_block_sizes([int(c)] * 6)
+            L.check(lib.sph_profile_reset())
+            for i in ids:
+                L.check(lib.sph_profile_enable(i, 1))
+            solve()
+            synchronize()
+            for k, i in enumerate(ids):
+                ms, n = C.c_double(), C.c_int64()
+                L.check(lib.sph_profile_read(i, C.byref(ms), C.byref(n)))
+                if n.value and (best[k] is None or ms.value / n.value < best[k]):
+                    best[k] = ms.value / n.value
+                    pick[k] = int(c)
+    finally:
+        for i in ids:
+            lib.sph_profile_enable(i, 0)
+        L.check(lib.sph_profile_reset())
+    state.set_block_sizes(pick)
+    return pick
 
 
 def synchronize():

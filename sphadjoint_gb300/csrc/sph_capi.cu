@@ -493,6 +493,28 @@ SPH_API int32_t sph_autotune(sph_state st, sph_field theta, int32_t reps, int32_
     });
 }
 
+SPH_API int32_t sph_set_block_sizes(sph_state st, const int32_t *blocks)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(blocks, "blocks");
+        int b[6];
+        for (int k = 0; k < 6; ++k) b[k] = blocks[k];
+        ST(st)->set_blocks(b);
+    });
+}
+
+SPH_API int32_t sph_get_block_sizes(sph_state st, int32_t *blocks)
+{
+    return guarded([&] {
+        need(st, "state");
+        need(blocks, "blocks");
+        int b[6];
+        ST(st)->get_blocks(b);
+        for (int k = 0; k < 6; ++k) blocks[k] = b[k];
+    });
+}
+
 SPH_API int32_t sph_set_group_lanes(int32_t lanes)
 {
     return guarded([&] {

@@ -139,6 +139,10 @@ class StateI {
     virtual int batch() const = 0;
     virtual void take_flags_batch(uint32_t *per_instance) = 0;
     virtual void autotune(FieldI *theta, int reps, int *chosen) = 0;
+    // threads per block of the six tuned kernels (build, density, accel,
+    // drag, pass 1, pass 2) for this state's precision and kind
+    virtual void set_blocks(const int *blocks) = 0;
+    virtual void get_blocks(int *blocks) const = 0;
 };
 
 enum ObjectiveKind : int32_t {

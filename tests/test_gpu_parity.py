@@ -194,6 +194,52 @@ def test_autotuned_block_sizes_do_not_change_results():
         assert np.array_equal(ref[k], again[k]), k
 
 
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_block_sizes_set_directly_or_in_solve_do_not_change_results(dtype):
+    # one thread per particle (the tuned kernels); every block size runs the
+    # same per-particle code, so results are bit-identical in both precisions
+    case = K.jittered_block_case(side=40, ntheta=16, seed=8)
+    rng = np.random.default_rng(4)
+    case["cX"] = rng.standard_normal(case["X0"].shape)
+    case["cV"] = rng.standard_normal(case["X0"].shape)
+    seeds = linear_seeds(case)
+    p = S.SPHParams(**case["p"], dtype=dtype)
+    st = S.State(case["X0"], case["V0"], p)
+    S.set_group_lanes(1)
+    try:
+        outs = []
+        for b in (64, 256, 128):
+            st.set_block_sizes([b] * 6)
+            assert st.block_sizes() == [b] * 6
+            outs.append(run_gpu(case, 12, dtype=dtype, seeds=seeds))
+        for o in outs[1:]:
+            for k in ("X", "V", "gX", "gV", "gtheta"):
+                assert np.array_equal(outs[0][k], o[k]), k
+        with pytest.raises(S.ArgumentError):
+            st.set_block_sizes([96] * 6)
+        th = S.DesignField(case["theta"], dtype)
+        tp = S.Tape(st.N, 8, p)
+        ws = S.AdjointWorkspace(st.N, p)
+        st0 = S.State(case["X0"], case["V0"], p)
+
+        def solve():
+            st.assign(st0)
+            tp.reset()
+            S.simulate(st, th, p, 8, tp)
+            ws.objective(st, "ke_right")
+            S.backward_seeded(ws, tp, th, p)
+
+        solve()
+        chosen = S.autotune_in_solve(st, solve)
+        assert st.block_sizes() == chosen and all(b in (64, 128, 256) for b in chosen)
+        again = run_gpu(case, 12, dtype=dtype, seeds=seeds)
+        for k in ("X", "V", "gX", "gV", "gtheta"):
+            assert np.array_equal(outs[0][k], again[k]), k
+    finally:
+        S.set_group_lanes(0)
+        st.set_block_sizes([256] * 6)
+
+
 def test_small_dambreak_full_horizon_bit_exact():
     """The reference's CPU case: 2072 particles, 5333 steps in FP64, KE of the
     right half. J, the final state and dJ/dX0, dJ/dV0 stay bit-identical to the
