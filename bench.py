@@ -39,6 +39,16 @@ sys.path.insert(0, ROOT)
 # steps of the short solves that choose the block sizes inside the solve
 TUNE_STEPS = 32
 
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 1,048,576
+# particles, FP32 (the --set full captures summarised in profiles/*_1M_fp32.md)
+TRAFFIC_1M_F32 = {
+    "density": 38.239488e6 + 1.775616e6,
+    "accel_integrate": 55.129088e6 + 1.536768e6,
+    "accel_drag": 71.912960e6 + 4.487680e6,
+    "pass1": 76.112128e6 + 4.829952e6,
+    "pass2": 63.410432e6 + 0.497664e6,
+}
+
 # algorithmic HBM bytes per particle per launch (compulsory traffic of the
 # minimal dataflow, s = sizeof(T)): read/write sets of each fused pass
 ALGO_WORDS = {
@@ -642,8 +652,9 @@ def run_ours(args):
     achieved = algo_bytes / (per_launch_ms / 1000.0) / 1e9
     roof = {"kernel": args.kernel, "bound": "hbm", "achieved": achieved, "peak": hbm,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": (args.traffic_bytes if args.traffic_bytes and args.kernel == "pass1"
-                        and N == 1 << 20 else None),
+            "traffic": (args.traffic_bytes if args.traffic_bytes
+                        else TRAFFIC_1M_F32.get(args.kernel)
+                        if N == 1 << 20 and args.dtype == "f32" else None),
             "algorithmic_bytes_per_launch": algo_bytes, "ms_per_launch": per_launch_ms,
             "launches": kn.value}
 
@@ -811,14 +822,15 @@ def main():
                     help="checkpoint slots, 0 = full tape (single: 32; batched: full tape)")
     ap.add_argument("--ntheta", type=int, default=256)
     ap.add_argument("--dtype", default="f32", choices=["f32", "f64"])
-    ap.add_argument("--kernel", default="pass1", choices=sorted(ALGO_WORDS))
+    ap.add_argument("--kernel", default="density", choices=sorted(ALGO_WORDS),
+                    help="the roofline's kernel (default: the largest share of the solve)")
     ap.add_argument("--kernel-events", type=int, default=1,
                     help="time --kernel with CUDA events inside the timed region (1) or on "
                          "one extra solve after it (0)")
-    ap.add_argument("--traffic-bytes", type=float, default=81.09e6,
-                    help="ncu dram read+write bytes of one launch of --kernel at the default "
-                         "size (k_pass1_design, 1,048,576 particles: 76.1 MB + 5.0 MB), "
-                         "reported as roofline.traffic; 0 = unknown")
+    ap.add_argument("--traffic-bytes", type=float, default=0.0,
+                    help="ncu dram read+write bytes of one launch of --kernel, reported as "
+                         "roofline.traffic; 0 = the captured figure at 1,048,576 FP32 "
+                         "particles (TRAFFIC_1M_F32), else unknown")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
