@@ -738,7 +738,9 @@ def autotune_in_solve(state, solve, candidates=(64, 128, 256)):
     forward+adjoint solve with ``state``'s precision and kind; it is called
     once per candidate with every tuned kernel at that size, each kernel's
     launches are timed with CUDA events, and each kernel keeps its fastest
-    size. Returns the chosen sizes (TUNED_KERNELS order).
+    size. Returns the chosen sizes (TUNED_KERNELS order). It uses the
+    library's kernel timers: they are reset, and the six kernels' timers are
+    off afterwards.
 
     Repeated launches of one kernel, as the engine's own autotune times them,
     can favour a size that is slower inside the solve's kernel sequence (on
