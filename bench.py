@@ -103,7 +103,9 @@ def small_workload():
     cfg = {"workload": "small dam break: 56x37 = 2072 particles, 5333 steps FP64, full tape, "
                        "theta 32x32 zeros", "particles": nx * ny, "time_steps": 5333,
            "snapshots": 0, "theta": [32, 32], "tank": [1.6, 1.0], "dx": dx, "skin": 0.2,
-           "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half"}
+           "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half",
+           "l2": "working set fits in L2 (2072 particles, ~1 MB per state); one timed step "
+                 "is a whole 5333-step solve whose tape (0.35 GB) streams through HBM"}
     return p, X0, np.zeros_like(X0), np.zeros((32, 32)), cfg
 
 
@@ -132,7 +134,8 @@ def dense_workload(side=2896, ntheta=512, seed=5):
                        "rebuilt every step, 200 steps FP32, 16 checkpoints, theta 512x512 "
                        "with 50% solid blobs", "particles": side * side, "time_steps": 200,
            "snapshots": 16, "theta": [ntheta, ntheta], "dx": sp, "skin": 0.2, "interval": 1,
-           "maxnb": 64, "objective": "kinetic energy, right half"}
+           "maxnb": 64, "objective": "kinetic energy, right half",
+           "l2": "inputs larger than L2 (8.4M particles: ~0.5 GB of per-particle arrays per pass)"}
     return p, X0, np.zeros_like(X0), theta, cfg
 
 
@@ -166,7 +169,9 @@ def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3, snapshots=0):
                        + ("full tape" if snapshots == 0 else f"{snapshots} checkpoint slots"),
            "instances": B, "particles": int(sum(x[1].shape[1] for x in inst)),
            "time_steps": nsteps, "snapshots": snapshots, "theta": [ntheta, ntheta], "dx": dx,
-           "skin": 0.2, "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half"}
+           "skin": 0.2, "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half",
+           "l2": "inputs larger than L2 (868,449 particles and a 27.8 GB full tape "
+                 "streamed per solve)"}
     return inst, cfg
 
 
