@@ -170,8 +170,8 @@ def batched_workload(B=64, nsteps=2000, ntheta=64, seed=3, snapshots=0):
            "instances": B, "particles": int(sum(x[1].shape[1] for x in inst)),
            "time_steps": nsteps, "snapshots": snapshots, "theta": [ntheta, ntheta], "dx": dx,
            "skin": 0.2, "interval": 4, "maxnb": 64, "objective": "kinetic energy, right half",
-           "l2": "inputs larger than L2 (868,449 particles and a 27.8 GB full tape "
-                 "streamed per solve)"}
+           "l2": "inputs larger than L2 (per-particle arrays of all instances, and the "
+                 "tape or checkpoints, stream through HBM every solve)"}
     return inst, cfg
 
 
