@@ -49,6 +49,14 @@ TRAFFIC_1M_F32 = {
     "pass2": 63.410432e6 + 0.497664e6,
 }
 
+# smsp__issue_active.avg.pct_of_peak_sustained_active of the same captures:
+# the fraction of cycles in which a warp scheduler issued, the bound these
+# gather kernels actually meet (HBM throughput stays in single digits)
+ISSUE_ACTIVE_1M_F32 = {
+    "density": 0.7828, "accel_integrate": 0.7166, "accel_drag": 0.6977,
+    "pass1": 0.7126, "pass2": 0.7513,
+}
+
 # algorithmic HBM bytes per particle per launch (compulsory traffic of the
 # minimal dataflow, s = sizeof(T)): read/write sets of each fused pass
 ALGO_WORDS = {
@@ -661,7 +669,9 @@ def run_ours(args):
                         else TRAFFIC_1M_F32.get(args.kernel)
                         if N == 1 << 20 and args.dtype == "f32" else None),
             "algorithmic_bytes_per_launch": algo_bytes, "ms_per_launch": per_launch_ms,
-            "launches": kn.value}
+            "launches": kn.value,
+            "issue_active_frac": (ISSUE_ACTIVE_1M_F32.get(args.kernel)
+                                  if N == 1 << 20 and args.dtype == "f32" else None)}
 
     # per-kernel breakdown of one more solve (untimed)
     kernels = {}
