@@ -85,6 +85,24 @@ def test_fp32_lane_groups_within_tolerance(lanes):
             assert K.relerr(o[k], r[k]) <= 1e-5, (g, k)
 
 
+def test_fp32_lane_groups_with_spilled_rows_within_tolerance(lanes):
+    # FP32 lane groups on the dense case: spilled particles' rows listed in
+    # shared memory, maxnb truncation; against the FP64 oracle and the
+    # one-thread FP32 form
+    case = dense_case()
+    seeds = linear_seeds(case)
+    r = run_oracle(case, 6, seeds=seeds, interval=2)
+    lanes(1)
+    one = run_gpu(case, 6, dtype="f32", seeds=seeds, interval=2)
+    for g in (16, 32):
+        lanes(g)
+        o = run_gpu(case, 6, dtype="f32", seeds=seeds, interval=2)
+        assert o["flags"] == r["flags"]
+        for k in ("X", "V", "gX", "gV", "gtheta"):
+            assert K.relerr(o[k], r[k]) <= 1e-5, (g, k)
+            assert K.relerr(o[k], one[k]) <= 1e-5, (g, k)
+
+
 def test_lane_setting_rejects_other_values():
     with pytest.raises(S.ArgumentError):
         S.set_group_lanes(8)
