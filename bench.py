@@ -747,14 +747,30 @@ def run_ours(args):
     # e2e: the reference-facing calls with host buffers
     e2e = None
     if args.e2e_steps > 0:
-        Xh = np.ascontiguousarray(X0.T, dtype=p.np)
-        Vh = np.ascontiguousarray(V0.T, dtype=p.np)
-        thh = np.asfortranarray(theta.astype(p.np))
-        outX = np.empty_like(Xh)
-        outV = np.empty_like(Vh)
-        gX = np.empty_like(Xh)
-        gV = np.empty_like(Vh)
-        gth = np.empty((p.ngx, p.ngy), p.np)
+        # host buffers in pinned (page-locked) memory, as a caller that
+        # streams solves would hold them; pageable numpy if pinning fails
+        keep = []
+        pinned_ok = [True]
+
+        def host(shape, order="C"):
+            try:
+                t = torch.empty(int(np.prod(shape)), pin_memory=True,
+                                dtype=torch.float64 if p.np == np.float64 else torch.float32)
+                keep.append(t)
+                return t.numpy().reshape(shape, order=order)
+            except RuntimeError:
+                pinned_ok[0] = False
+                return np.empty(shape, p.np, order=order)
+
+        Xh = host(X0.T.shape)
+        Xh[...] = X0.T
+        Vh = host(V0.T.shape)
+        Vh[...] = V0.T
+        thh = host(theta.shape, order="F")
+        thh[...] = theta
+        outX, outV, gX, gV = (host(Xh.shape) for _ in range(4))
+        sV = host(Vh.shape)
+        gth = host((p.ngx, p.ngy))
 
         def solve_host():
             h = C.c_void_p()
@@ -767,7 +783,8 @@ def run_ours(args):
             LB.check(L.sph_state_get(h, outX.ctypes.data_as(C.c_void_p),
                                      outV.ctypes.data_as(C.c_void_p)))
             right = outX[:, 0] > p.Lx / 2
-            sV = np.where(right[:, None], p.m * outV, 0).astype(p.np)
+            np.multiply(outV, p.np(p.m), out=sV)
+            sV[~right] = 0
             LB.check(L.sph_backward(ws.h, tape.h, th.h, C.byref(pc), None,
                                     sV.ctypes.data_as(C.c_void_p), None, 0.2, interval, 64,
                                     C.byref(flags)))
@@ -787,7 +804,8 @@ def run_ours(args):
         d2h = outX.nbytes + outV.nbytes + gX.nbytes + gV.nbytes + gth.nbytes
         e2e = {"value": N * args.nsteps * world / te, "unit": "particle-steps/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "ms_per_step": 1000 * te, "steps": args.e2e_steps}
+               "ms_per_step": 1000 * te, "steps": args.e2e_steps,
+               "pinned_host_buffers": pinned_ok[0]}
 
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
