@@ -78,3 +78,40 @@ def test_layout_keyword_is_validated_like_the_reference():
         A._check_layout(ok)
     with pytest.raises(LB.ArgumentError):
         A._check_layout("columns")
+
+
+def test_header_is_plain_c_and_links(lib, tmp_path):
+    # the boundary as a C caller (cgo, Julia ccall, JNI) sees it: the header
+    # compiles as C99 and a C program links against the library and calls
+    # host-only entry points (no device work)
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include "sphadjoint_gb300.h"
+int main(void) {
+    sph_params p = {0};
+    int32_t lanes = -1;
+    if (sph_version() <= 0) return 1;
+    if (sph_plan_cost(1000, 32) != 2405) return 2;
+    if (sph_set_group_lanes(8) != SPH_ERR_ARG || sph_last_error()[0] == 0) return 3;
+    if (sph_get_group_lanes(&lanes) != SPH_OK || lanes != 0) return 4;
+    (void)p;
+    printf("ok\n");
+    return 0;
+}
+""")
+    exe = tmp_path / "abi"
+    libdir = os.path.dirname(lib._name)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe), "-L", libdir, "-lsphgb300",
+                        "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
+
