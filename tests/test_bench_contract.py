@@ -44,6 +44,27 @@ def test_reference_arm_line():
     assert d["e2e"]["value"] == d["value"] == d["cpu_baseline"]["value"]
 
 
+def test_reference_arm_under_torchrun_prints_one_line_from_rank_0():
+    # launched like the scaling runs: rank 0 times the CPU path, the other
+    # rank exits 0 without work
+    import socket
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+                          "--nproc-per-node", "2", "--master-addr", "127.0.0.1",
+                          "--master-port", str(port), os.path.join(ROOT, "bench.py"),
+                          "--impl", "reference", "--gpus", "2", "--side", "24", "--nsteps", "8",
+                          "--steps", "1", "--warmup", "1", "--ref-step-seconds", "0.3"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
 @pytest.mark.gpu
 def test_gpu_arm_line():
     d = run_bench("--side", "48", "--nsteps", "16", "--snapshots", "4", "--steps", "1",
