@@ -489,7 +489,7 @@ def cpu_sample(p, X0, V0, theta, dtype, budget_s=12.0, max_steps=64, interval=4)
     n = int(max(1, min(max_steps, budget_s / max(t1, 1e-3))))
     t = run(n) if n > 1 else t1
     return {"value": N * n / t, "unit": "particle-steps/s", "cores": O.get_threads(),
-            "kind": "port",
+            "kind": "port", "time_steps": n,
             "sample": f"{N} particles x {n} time steps, forward + adjoint with a full tape, "
                       f"{dtype.upper()}, C restatement of the reference with OpenMP",
             "seconds": t}
@@ -550,6 +550,13 @@ def run_reference(args):
             "cpu_baseline": {k: last[k] for k in ("unit", "cores", "kind", "sample")} | {"value": v},
             "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
+            "horizon": {"sampled_time_steps": last["time_steps"], "sampled_tape": "full",
+                        "configured_time_steps": args.nsteps,
+                        "configured_snapshots": args.snapshots,
+                        "note": "each step times the first sampled_time_steps steps of the "
+                                "workload, forward + adjoint with a full tape (no checkpoint "
+                                "recomputation), normalised per particle-step; the GPU arm runs "
+                                "the configured horizon with checkpoint recomputation"},
             "note": "the reference is Julia (KernelAbstractions); Julia is not installed, so its "
                     "CPU path is timed through the C restatement in oracle/"}
     print(json.dumps(line))
@@ -737,12 +744,38 @@ def run_ours(args):
         J64 = ws64.objective(st64, "ke_right")
         S.backward_seeded(ws64, tp64, th64, p64, interval=interval)
         r64 = grab(st64, ws64)
-        fp64 = {"seconds": time.perf_counter() - t0, "J_f32": J32, "J_f64": J64,
+        fp64 = {"seconds": time.perf_counter() - t0, "time_steps": args.nsteps,
+                "objective": "kinetic energy, right half", "J_f32": J32, "J_f64": J64,
                 "J_rel": abs(J32 - J64) / abs(J64)}
         for k in r64:
             fp64[k + "_rel"] = float(np.max(np.abs(r32[k] - r64[k])) /
                                      max(np.max(np.abs(r64[k])), 1e-300))
         del st64, tp64, ws64
+        # The same comparison where the problem is still well conditioned: 10
+        # steps of the smooth target objective centred in the block (the
+        # right-half kinetic energy counts particles with x > Lx/2, and this
+        # state's last lattice column sits on that line). IEEE FP32 itself
+        # stays within 1e-5 of FP64 here on X, dJ/dX0, dJ/dV0 and J.
+        H = N ** 0.5 * cfg["dx"]
+        targs = (0.5 * H, 0.4 * H, 0.15 * H)
+        short = {"time_steps": 10, "objective": "target_objective, centre (0.5H, 0.4H), "
+                                                "sigma 0.15H"}
+        res = {}
+        for dt in ("f32", "f64"):
+            pp = S.SPHParams(**p_d, dtype=dt)
+            s_ = S.State(X0, V0, pp, interval=interval)
+            t_ = S.Tape(N, 10, pp, snapshots=0)
+            w_ = S.AdjointWorkspace(N, pp)
+            S.simulate(s_, S.DesignField(theta, dt), pp, 10, t_)
+            Jv = w_.objective(s_, "target", targs)
+            S.backward_seeded(w_, t_, S.DesignField(theta, dt), pp, interval=interval)
+            res[dt] = grab(s_, w_) | {"J": Jv}
+            del s_, t_, w_
+        for k in ("X", "V", "gX", "gV", "gtheta"):
+            short[k + "_rel"] = float(np.max(np.abs(res["f32"][k] - res["f64"][k])) /
+                                      max(np.max(np.abs(res["f64"][k])), 1e-300))
+        short["J_rel"] = abs(res["f32"]["J"] - res["f64"]["J"]) / abs(res["f64"]["J"])
+        fp64["well_conditioned"] = short
 
     # e2e: the reference-facing calls with host buffers
     e2e = None
@@ -868,15 +901,18 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-step-seconds", type=float, default=8.0)
     ap.add_argument("--breakdown", type=int, default=1)
-    ap.add_argument("--fp64-check", type=int, default=0,
+    ap.add_argument("--fp64-check", type=int, default=-1,
                     help="also solve the workload in FP64 on the GPU and report the FP32 "
-                         "results' relative difference")
+                         "results' relative difference (the full horizon, and 10 steps of a "
+                         "smooth objective); default: on for the single workload")
     ap.add_argument("--graph", type=int, default=0,
                     help="time replays of the whole solve captured as one CUDA graph")
     ap.add_argument("--autotune", type=int, default=1,
                     help="measure per-kernel block sizes on the workload before timing")
     args = ap.parse_args()
     batched = args.workload == "batched"
+    if args.fp64_check < 0:
+        args.fp64_check = 1 if args.workload == "single" else 0
     if args.nsteps is None:
         args.nsteps = 2000 if batched else 1000
     if args.snapshots is None:

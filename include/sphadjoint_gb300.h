@@ -30,7 +30,7 @@ extern "C" {
 
 #define SPH_API __attribute__((visibility("default")))
 
-/* SPHParams{T} (src/params.jl:58-72). gx/gy default to 0 / -9.81 there.
+/* SPHParams{T} (src/params.jl:14-28). gx/gy default to 0 / -9.81 there.
    The trailing fields select model variants that have no counterpart in the
    reference (which has the linear EOS and Morris viscosity, README.md:505-519);
    all zero = the reference's model:
@@ -130,6 +130,25 @@ SPH_API int32_t sph_tape_create(int64_t N, int64_t nsteps, int32_t dtype, sph_ta
    src/driver.jl:56-60 names it as the next step). */
 SPH_API int32_t sph_tape_create_checkpointed(int64_t N, int64_t nsteps, int32_t nsnapshots,
                                              int32_t dtype, sph_tape *out);
+/* Tape mode chosen from a device-memory budget (no counterpart in the
+   reference, whose Tape stores every step; src/driver.jl:56-60 names
+   checkpointing as the way beyond that size). The full tape when its
+   2 * 2 * sizeof(T) * N * nsteps bytes fit in budget_bytes; otherwise binomial
+   checkpointing with as many snapshots as fit beside the recompute state (at
+   most nsteps - 1: more would not save a recomputed step). A snapshot holds
+   the state's core arrays and cell table, whose size follows from p (Lx, Ly,
+   h) and skin. budget_bytes < 0: 90% of the device's free memory at the call.
+   *nsnapshots: 0 = full tape; *bytes: the tape's device bytes (either may be
+   NULL). SPH_ERR_NOMEM when not even one snapshot fits. sph_tape_plan only
+   plans (host only when budget_bytes >= 0); sph_tape_create_auto creates the
+   tape it plans, and sph_tape_snapshots reads a tape's mode back. */
+SPH_API int32_t sph_tape_plan(const sph_params *p, int64_t N, int64_t nsteps, int32_t dtype,
+                              double skin, int64_t budget_bytes, int32_t *nsnapshots,
+                              int64_t *bytes);
+SPH_API int32_t sph_tape_create_auto(const sph_params *p, int64_t N, int64_t nsteps,
+                                     int32_t dtype, double skin, int64_t budget_bytes,
+                                     sph_tape *out);
+SPH_API int32_t sph_tape_snapshots(sph_tape tp, int32_t *nsnapshots);
 SPH_API int32_t sph_tape_destroy(sph_tape tp);
 /* reset!(tape) (src/driver.jl:71) */
 SPH_API int32_t sph_tape_reset(sph_tape tp);
@@ -260,8 +279,11 @@ SPH_API int64_t sph_request_bytes(const sph_request *req, int32_t dtype);
    larger sizes return SPH_ERR_ARG. Calls no cudaMalloc/cudaFree. Enqueued on
    `stream` (a cudaStream_t, NULL = legacy default) and not synchronised.
    All calls share the work array: calls that overlap on the GPU race, so
-   serialise them. The first call on each device resolves the array's address
-   (cudaGetSymbolAddress): make it before any stream capture. */
+   serialise them. Each call outside a stream capture resolves the array's
+   device address (cudaGetSymbolAddress on the current device); a call while
+   `stream` is captured reuses the last one, so make one uncaptured call on
+   each device before capturing. A CUDA error already pending when the call
+   starts is reported (SPH_ERR_CUDA) and nothing is launched. */
 #define SPH_NOALLOC_MAX_PARTICLES (1 << 20)
 #define SPH_NOALLOC_MAX_CELLS (1 << 20)
 SPH_API int32_t sph_build_cells_noalloc(const void *X_dev, int64_t N, int32_t dtype, double cs,

@@ -128,7 +128,7 @@ R FN(orc_g_kern)(R q, R A, R h)
     return (R)0;
 }
 
-/* ---- src/params.jl:80-90 -------------------------------------------------- */
+/* ---- src/params.jl:36-46 -------------------------------------------------- */
 static inline R FN(wall_accel)(R x, R L, R kw)
 {
     R lo = (-x > (R)0) ? -x : (R)0;        /* max(zero(T), -x) */
@@ -143,7 +143,7 @@ static inline R FN(wall_daccel)(R x, R L, R kw)
     return kw * ((R)(-2) * lo - (R)2 * hi);
 }
 
-/* ---- src/params.jl:98-126 ------------------------------------------------- */
+/* ---- src/params.jl:54-82 ------------------------------------------------- */
 static inline R FN(clampR)(R x, R lo, R hi)
 {
     /* Base.clamp: ifelse(x > hi, hi, ifelse(x < lo, lo, x)) */

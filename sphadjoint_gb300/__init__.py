@@ -31,6 +31,7 @@ from .api import (  # noqa: F401
     step,
     synchronize,
     target_objective,
+    tape_plan,
 )
 from ._lib import SPHError, CapacityError, ArgumentError, load  # noqa: F401
 

@@ -86,6 +86,9 @@ _SIGS = {
     "sph_simulate": (_I32, [_P, _P, _SP, _I64, _P, _U32P]),
     "sph_tape_create": (_I32, [_I64, _I64, _I32, _PP]),
     "sph_tape_create_checkpointed": (_I32, [_I64, _I64, _I32, _I32, _PP]),
+    "sph_tape_plan": (_I32, [_SP, _I64, _I64, _I32, C.c_double, _I64, _I32P, _I64P]),
+    "sph_tape_create_auto": (_I32, [_SP, _I64, _I64, _I32, C.c_double, _I64, _PP]),
+    "sph_tape_snapshots": (_I32, [_P, _I32P]),
     "sph_tape_destroy": (_I32, [_P]),
     "sph_tape_reset": (_I32, [_P]),
     "sph_tape_length": (_I32, [_P, _I64P]),
@@ -130,6 +133,8 @@ _SIGS = {
     "sph_profile_reset": (_I32, []),
     "sph_plan_cost": (_I64, [_I64, _I64]),
     "sph_plan_split": (_I64, [_I64, _I64]),
+    "sph_build_cells_noalloc": (_I32, [_P, _I64, _I32, C.c_double, _I32, _I32, _I32P, _I32P,
+                                       _I32P, _P]),
 }
 
 

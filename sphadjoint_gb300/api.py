@@ -1,6 +1,6 @@
 """Python mirror of SPHAdjoint's public API over the C ABI.
 
-Names follow the reference module's exports (src/SPHAdjoint.jl:212-213):
+Names follow the reference module's exports (src/SPHAdjoint.jl:39-40):
 ``SPHParams, State, Tape, AdjointWorkspace, simulate, step, build,
 build_neighbors, backward, target_objective, reset`` (Julia's ``simulate!``
 is ``simulate`` here, etc.). Arrays use the reference's shapes: positions,
@@ -22,7 +22,7 @@ _DT = {"f64": (L.SPH_F64, np.float64), "f32": (L.SPH_F32, np.float32)}
 
 @dataclass
 class SPHParams:
-    """SPHParams{T} (src/params.jl:58-72); ``dtype`` is T ("f64" or "f32").
+    """SPHParams{T} (src/params.jl:14-28); ``dtype`` is T ("f64" or "f32").
 
     ``eos`` and ``visc`` select model variants that the reference does not
     have (it uses the linear EOS and Morris viscosity): ``eos="tait"`` with
@@ -72,7 +72,7 @@ class SPHParams:
     def np(self):
         return _DT[self.dtype][1]
 
-    # src/params.jl:74-76
+    # src/params.jl:30-32
     def support(self) -> float:
         return 2 * self.h
 
@@ -259,17 +259,29 @@ class Tape:
     ``snapshots=0`` keeps every step's (X, V) like the reference. ``snapshots=c``
     keeps c device snapshots and recomputes the rest during ``backward``
     (binomial checkpointing), for horizons whose full history would not fit.
+    ``snapshots="auto"`` picks the full tape when it fits in ``budget_bytes``
+    (default: 90% of the device's free memory) and otherwise as many snapshots
+    as fit; ``self.snapshots`` holds the choice.
     """
 
-    def __init__(self, N: int, nsteps: int, p: SPHParams, snapshots: int = 0):
+    def __init__(self, N: int, nsteps: int, p: SPHParams, snapshots=0, budget_bytes=None,
+                 skin=0.2):
         self._L = L.load()
-        self.N, self.cap, self.p, self.snapshots = int(N), int(nsteps), p, int(snapshots)
+        self.N, self.cap, self.p = int(N), int(nsteps), p
         h = C.c_void_p()
-        if snapshots:
+        if snapshots == "auto":
+            budget = -1 if budget_bytes is None else int(budget_bytes)
+            L.check(self._L.sph_tape_create_auto(C.byref(p.c_struct()), self.N, self.cap, p.code,
+                                                 float(skin), budget, C.byref(h)))
+            c = C.c_int32()
+            L.check(self._L.sph_tape_snapshots(h, C.byref(c)))
+            snapshots = c.value
+        elif snapshots:
             L.check(self._L.sph_tape_create_checkpointed(self.N, self.cap, int(snapshots), p.code,
                                                          C.byref(h)))
         else:
             L.check(self._L.sph_tape_create(self.N, self.cap, p.code, C.byref(h)))
+        self.snapshots = int(snapshots)
         self.h = h
 
     def __del__(self):
@@ -299,6 +311,16 @@ class Tape:
         n = C.c_int64()
         L.check(self._L.sph_tape_recomputed_steps(self.h, C.byref(n)))
         return n.value
+
+
+def tape_plan(N: int, nsteps: int, p: SPHParams, budget_bytes: int, skin=0.2):
+    """(snapshots, device bytes) of the tape ``Tape(..., snapshots="auto")``
+    would create under ``budget_bytes``: 0 snapshots = the full tape."""
+    lib = L.load()
+    c, b = C.c_int32(), C.c_int64()
+    L.check(lib.sph_tape_plan(C.byref(p.c_struct()), int(N), int(nsteps), p.code, float(skin),
+                              int(budget_bytes), C.byref(c), C.byref(b)))
+    return c.value, b.value
 
 
 class AdjointWorkspace:

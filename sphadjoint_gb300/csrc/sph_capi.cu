@@ -418,6 +418,107 @@ SPH_API int32_t sph_tape_create_checkpointed(int64_t N, int64_t nsteps, int32_t 
     });
 }
 
+// Device bytes of the two tape modes of one state (the layouts of Sys and
+// Tape in sph_engine.cuh): a snapshot is the state's contiguous core block
+// (positions and velocities in both buffers, rebuild positions, permutation,
+// inverse, cell centres, six mask words, cell starts), and a checkpoint tape
+// also holds a recompute state (the core plus the neighbour-list work arrays,
+// in-support masks, densities and staging).
+static int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
+
+static void tape_sizes(const sph_params *p, int64_t N, int32_t dtype, double skin, int64_t *snap,
+                       int64_t *recomp)
+{
+    const int64_t s = dtype == SPH_F64 ? 8 : 4;
+    const int64_t n1 = std::max<int64_t>(N, 1);
+    // cell grid as State builds it: rc = Float64(T(2) T(h)) (1 + skin),
+    // nx = ceil(Lx / rc) + 2 (src/neighbors.jl:28-36)
+    const double hT = dtype == SPH_F64 ? p->h : (double)(float)p->h;
+    const double rc = (dtype == SPH_F64 ? 2.0 * hT : (double)(2.0f * (float)hT)) * (1.0 + skin);
+    const double LxT = dtype == SPH_F64 ? p->Lx : (double)(float)p->Lx;
+    const double LyT = dtype == SPH_F64 ? p->Ly : (double)(float)p->Ly;
+    const int64_t nx = (int64_t)std::max(1.0, std::ceil(LxT / rc) + 2);
+    const int64_t ny = (int64_t)std::max(1.0, std::ceil(LyT / rc) + 2);
+    const int64_t ncell = nx * ny;
+    *snap = 5 * align256(2 * s * n1) + 3 * align256(4 * n1) + align256(24 * n1) +
+            align256(4 * (ncell + 1));
+    *recomp = *snap + (16 + 24 + 6 * s) * n1 + 8 * ncell + 4 * (ncell / 2048 + 2) + 4;
+}
+
+static int64_t device_budget()
+{
+    size_t fr = 0, tot = 0;
+    cuda_check(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo");
+    return (int64_t)(0.9 * (double)fr);
+}
+
+static void tape_plan(const sph_params *p, int64_t N, int64_t nsteps, int32_t dtype, double skin,
+                      int64_t budget, int32_t *nsnap, int64_t *bytes)
+{
+    if (N < 0 || nsteps < 0) throw Error(ERR_ARG, "negative tape size");
+    const int64_t s = dtype == SPH_F64 ? 8 : 4;
+    const int64_t L = std::max<int64_t>(nsteps, 1);
+    const int64_t full = 4 * s * std::max<int64_t>(N, 1) * L;
+    if (full <= budget || L <= 1) {
+        *nsnap = 0;
+        *bytes = full;
+        return;
+    }
+    int64_t snap = 0, recomp = 0;
+    tape_sizes(p, N, dtype, skin, &snap, &recomp);
+    const int64_t c = budget > recomp ? std::min<int64_t>((budget - recomp) / snap, L - 1) : 0;
+    if (c < 1)
+        throw Error(ERR_NOMEM, "tape of " + std::to_string(N) + " particles x " +
+                                   std::to_string(nsteps) + " steps: not even one snapshot (" +
+                                   std::to_string((snap + recomp) >> 20) + " MiB with the "
+                                   "recompute state) fits in " + std::to_string(budget >> 20) +
+                                   " MiB");
+    *nsnap = (int32_t)std::min<int64_t>(c, INT32_MAX);
+    *bytes = *nsnap * snap + recomp;
+}
+
+SPH_API int32_t sph_tape_plan(const sph_params *p, int64_t N, int64_t nsteps, int32_t dtype,
+                              double skin, int64_t budget_bytes, int32_t *nsnapshots,
+                              int64_t *bytes)
+{
+    return guarded([&] {
+        need(p, "params");
+        check_dtype(dtype);
+        int32_t c = 0;
+        int64_t b = 0;
+        tape_plan(p, N, nsteps, dtype, skin, budget_bytes < 0 ? device_budget() : budget_bytes,
+                  &c, &b);
+        if (nsnapshots) *nsnapshots = c;
+        if (bytes) *bytes = b;
+    });
+}
+
+SPH_API int32_t sph_tape_create_auto(const sph_params *p, int64_t N, int64_t nsteps,
+                                     int32_t dtype, double skin, int64_t budget_bytes,
+                                     sph_tape *out)
+{
+    return guarded([&] {
+        need(out, "out");
+        need(p, "params");
+        check_dtype(dtype);
+        int32_t c = 0;
+        int64_t b = 0;
+        tape_plan(p, N, nsteps, dtype, skin, budget_bytes < 0 ? device_budget() : budget_bytes,
+                  &c, &b);
+        TapeI *t = dtype == SPH_F64 ? make_tape_f64(N, nsteps, c) : make_tape_f32(N, nsteps, c);
+        *out = reinterpret_cast<sph_tape>(t);
+    });
+}
+
+SPH_API int32_t sph_tape_snapshots(sph_tape tp, int32_t *nsnapshots)
+{
+    return guarded([&] {
+        need(tp, "tape");
+        need(nsnapshots, "nsnapshots");
+        *nsnapshots = TP(tp)->snapshots();
+    });
+}
+
 SPH_API int32_t sph_tape_destroy(sph_tape tp)
 {
     return guarded([&] { delete TP(tp); });

@@ -4,8 +4,8 @@
 // FP64 build (compiled with --fmad=false, IEEE division and sqrt) reproduces
 // the reference's rounding bit for bit:
 //   Wendland C2 kernel ............ src/kernels.jl:15-44
-//   relu^2 wall and its derivative  src/params.jl:80-90
-//   bilinear design field alpha(x)  src/params.jl:98-126
+//   relu^2 wall and its derivative  src/params.jl:36-46
+//   bilinear design field alpha(x)  src/params.jl:54-82
 // The FP32 build uses the same source with multiply-add contraction enabled.
 #pragma once
 
@@ -57,7 +57,7 @@ __device__ __forceinline__ int select_bit(uint32_t m, int r)
     return pos;
 }
 
-// SPHParams{T} (src/params.jl:58-72) plus the constants each reference kernel
+// SPHParams{T} (src/params.jl:14-28) plus the constants each reference kernel
 // forms from it, formed on the host in T with the same association:
 //   A = T(7)/(T(4)*T(pi)*h^2), invh = 1/h, r2max = T(4)*h*h,
 //   Fc = -5*A*invh*invh, Gc = T(7.5)*A*invh*invh, twomumass = 2*m*mu,
@@ -248,7 +248,7 @@ template <typename T> __host__ __device__ __forceinline__ int cell_coord(T v, in
     return c > n ? n : c;
 }
 
-// wall_accel / wall_daccel (src/params.jl:80-90); max(zero(T), -x) keeps +0.
+// wall_accel / wall_daccel (src/params.jl:36-46); max(zero(T), -x) keeps +0.
 template <typename T> __device__ __forceinline__ T wall_accel(T x, T L, T kw)
 {
     const T lo = (-x > (T)0) ? -x : (T)0;
@@ -263,7 +263,7 @@ template <typename T> __device__ __forceinline__ T wall_daccel(T x, T L, T kw)
     return kw * ((T)(-2) * lo - (T)2 * hi);
 }
 
-// interp_cell (src/params.jl:98-112), 0-based i0, j0.
+// interp_cell (src/params.jl:54-68), 0-based i0, j0.
 template <typename T>
 __device__ __forceinline__ void interp_cell(T x, T y, const Phys<T> &p, int &i0, int &j0, T &fx,
                                             T &fy, T &ax, T &ay)
@@ -285,7 +285,7 @@ __device__ __forceinline__ void interp_cell(T x, T y, const Phys<T> &p, int &i0,
     fy = gyc - (T)b;
 }
 
-// interp_alpha (src/params.jl:115-126); theta is (ngy, ngx) column-major.
+// interp_alpha (src/params.jl:71-82); theta is (ngy, ngx) column-major.
 template <typename T>
 __device__ __forceinline__ void interp_alpha(const T *theta, T x, T y, const Phys<T> &p, T &a,
                                              T &dadx, T &dady)

@@ -12,7 +12,7 @@
 
 namespace sphgb {
 
-// SPHParams (src/params.jl:58-72); fields are converted to T by the engine.
+// SPHParams (src/params.jl:14-28); fields are converted to T by the engine.
 // eos / gamma / visc / alpha select the model variants (no counterpart in the
 // reference): eos 0 linear, 1 Tait with integer exponent gamma; visc 0 Morris,
 // 1 Monaghan artificial viscosity with coefficient alpha.

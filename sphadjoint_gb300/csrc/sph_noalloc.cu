@@ -19,9 +19,13 @@
 //     this entry point writes every word it reads before reading it, and zeroes
 //     the caller's `counts` itself. Calls that overlap on the GPU (two streams,
 //     or two host threads) race on the array: serialise them.
-//   * The first call on each device resolves the array's device address with
-//     cudaGetSymbolAddress (with that device current). Make that first call
-//     before any stream capture.
+//   * Each call resolves the array's device address with cudaGetSymbolAddress
+//     on the current device, so the address stays right after a
+//     cudaDeviceReset. While `stream` is being captured into a CUDA graph the
+//     call uses the address from its last uncaptured call on that device
+//     instead: make one uncaptured call on each device before capturing.
+//   * A CUDA error already pending when the call starts (left by other code)
+//     is reported as such, and nothing is launched.
 #include <mutex>
 #include <string>
 
@@ -52,20 +56,29 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 int32_t *g_ptr[kMaxDevices] = {};
 
-// Device address of g_scratch on the current device (resolved once per device).
-int32_t *scratch_ptr(int dev)
+// Device address of g_scratch on the current device: resolved on every call
+// outside a stream capture (cheap, and right after a context reset), taken
+// from the last such call while `s` is being captured.
+int32_t *scratch_ptr(int dev, cudaStream_t s)
 {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cuda_check(cudaStreamIsCapturing(s, &cap), "cudaStreamIsCapturing");
     std::lock_guard<std::mutex> g(g_mu);
-    if (!g_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-        if (e != cudaSuccess || !p) {
-            (void)cudaGetLastError();
-            throw Error(ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") +
-                                      cudaGetErrorString(e));
-        }
-        g_ptr[dev] = static_cast<int32_t *>(p);
+    if (cap != cudaStreamCaptureStatusNone) {
+        if (!g_ptr[dev])
+            throw Error(ERR_STATE, "sph_build_cells_noalloc: make one call on this device "
+                                   "outside stream capture first (it resolves the work "
+                                   "array's device address)");
+        return g_ptr[dev];
     }
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess || !p) {
+        (void)cudaGetLastError();
+        throw Error(ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") +
+                                  cudaGetErrorString(e));
+    }
+    g_ptr[dev] = static_cast<int32_t *>(p);
     return g_ptr[dev];
 }
 
@@ -128,10 +141,17 @@ template <typename T>
 void build_cells_noalloc(const void *X, int64_t N, double cs, int nx, int ny, int32_t *counts,
                          int32_t *starts, int32_t *order, cudaStream_t s)
 {
+    // an error left pending by other code is not this call's failure: report
+    // it as pending and launch nothing
+    const cudaError_t pend = cudaPeekAtLastError();
+    if (pend != cudaSuccess)
+        throw Error(ERR_CUDA, std::string("sph_build_cells_noalloc: a CUDA error was already "
+                                          "pending before the call: ") +
+                                  cudaGetErrorString(pend));
     int dev = 0;
     cuda_check(cudaGetDevice(&dev), "cudaGetDevice");
     if (dev < 0 || dev >= kMaxDevices) throw Error(ERR_ARG, "device ordinal out of range");
-    int32_t *w = scratch_ptr(dev);
+    int32_t *w = scratch_ptr(dev, s);
     const int64_t ncell = (int64_t)nx * ny;
     int32_t *cellTmp = w + kOffCell, *src = w + kOffSrc, *start = w + kOffStart;
     int32_t *cursor = w + kOffCursor, *scan = w + kOffScan;

@@ -8,8 +8,9 @@ line by line like src/adjoint.jl). Both use the older *explicit* Brinkman drag
 an explicit-drag switch so that these vectors pin its pair formulas, wall,
 design-field interpolation and time-loop adjoint.
 
-This script imports those tools from a checkout of the reference (default
-``/root/reference``, override with ``SPHADJOINT_REF``) and writes
+This script imports those tools from a checkout of the reference, whose path
+is the first argument or the ``SPHADJOINT_REF`` environment variable (one of
+them is required), and writes
 ``golden_verify.npz`` beside itself. It needs numpy and torch; the tests only
 read the committed ``.npz``.
 """
@@ -24,7 +25,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def _import_tools():
-    ref = os.environ.get("SPHADJOINT_REF", "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPHADJOINT_REF")
+    if not ref:
+        sys.exit("usage: gen_golden.py <reference checkout> (or set SPHADJOINT_REF)")
     sys.path.insert(0, os.path.join(ref, "tools"))
     import verify_adjoint as va  # noqa: E402
     import verify_gather as vg  # noqa: E402

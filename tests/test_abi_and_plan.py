@@ -115,3 +115,40 @@ int main(void) {
     r = subprocess.run([str(exe)], capture_output=True, text=True)
     assert r.returncode == 0 and r.stdout.strip() == "ok", (r.returncode, r.stdout, r.stderr)
 
+
+
+def test_tape_mode_follows_the_memory_budget():
+    """The automatic tape mode (host only with an explicit budget): the full
+    tape whenever its 4 sizeof(T) N L bytes fit, otherwise the most snapshots
+    that fit beside the recompute state, capped at L - 1; fewer bytes never
+    buy fewer recomputed steps; a budget below one snapshot is refused."""
+    import sphadjoint_gb300 as S
+    from sphadjoint_gb300 import _lib as LB
+
+    p = S.SPHParams(h=1.3e-3, m=1e-3, rho0=1000.0, c=20.0, mu=0.02, dt=1e-5, Lx=2.048,
+                    Ly=1.28, kw=5e4, ngx=256, ngy=256, dtype="f32")
+    N, L = 1 << 20, 1000
+    full = 4 * 4 * N * L
+    assert S.tape_plan(N, L, p, full) == (0, full)
+    assert S.tape_plan(N, L, p, 10 * full) == (0, full)
+    last_c, last_cost = None, None
+    for budget in (full - 1, full // 2, full // 8, full // 32, full // 60):
+        c, b = S.tape_plan(N, L, p, budget)
+        assert 1 <= c <= L - 1 and b <= budget
+        # one more snapshot would not have fitted
+        c2, _ = S.tape_plan(N, L, p, b + 1)
+        assert c2 == c
+        cost = LB.load().sph_plan_cost(L, c)
+        if last_c is not None:
+            assert c <= last_c and cost >= last_cost
+        last_c, last_cost = c, cost
+    # 16 GB FP32 full tape of the benchmark workload vs a 4 GB budget
+    c, _ = S.tape_plan(N, L, p, 4 << 30)
+    assert 32 <= c <= 60
+    with pytest.raises(S.SPHError) as e:
+        S.tape_plan(N, L, p, 1 << 20)
+    assert e.value.code == 5
+    # FP64 doubles the full tape
+    import dataclasses
+    p64 = dataclasses.replace(p, dtype="f64")
+    assert S.tape_plan(N, L, p64, 2 * full) == (0, 2 * full)

@@ -36,6 +36,9 @@ def _noalloc(lib, X0, dtype, grid, stream):
     counts = torch.full((nx * ny,), -7, dtype=torch.int32, device="cuda")
     starts = torch.full((nx * ny,), -7, dtype=torch.int32, device="cuda")
     order = torch.full((max(N, 1),), -7, dtype=torch.int32, device="cuda")
+    # the inputs and the -7 fills were queued on torch's current stream: the
+    # library's stream must wait for them, as any caller's stream would
+    stream.wait_stream(torch.cuda.current_stream())
     code = lib.sph_build_cells_noalloc(
         C.c_void_p(X.data_ptr()), N, 0 if dtype == "f64" else 1, C.c_double(cs), nx, ny,
         C.cast(C.c_void_p(counts.data_ptr()), C.POINTER(C.c_int32)),
@@ -72,6 +75,35 @@ def test_noalloc_matches_allocating_build_twice(dtype):
     ref, grid = _reference_celllist(case, dtype)
     counts, starts, order = _noalloc(lib, case["X0"], dtype, grid, stream)
     assert np.array_equal(order, ref["order"]) and np.array_equal(counts, ref["counts"])
+
+
+def _grid_case(nx, ny, N, seed):
+    """N random particles in a tank whose cell grid is exactly nx x ny (the
+    reference's nx = ceil(L / cs) + 2 with cs = 2h (1 + skin))."""
+    rng = np.random.default_rng(seed)
+    h = 1.3e-3
+    cs = 2 * h * 1.2
+    p = dict(h=h, m=1e-3, rho0=1000.0, c=20.0, mu=0.02, dt=1e-5, Lx=(nx - 2.5) * cs,
+             Ly=(ny - 2.5) * cs, kw=5e4, ngx=8, ngy=8)
+    X0 = np.vstack([rng.random(N) * p["Lx"], rng.random(N) * p["Ly"]])
+    return dict(p=p, X0=X0, V0=np.zeros_like(X0), theta=np.zeros((8, 8)))
+
+
+@pytest.mark.parametrize("nx,ny,N", [(96, 80, 100_000), (1024, 1024, 1 << 20)])
+def test_noalloc_multi_block_scan_and_limits(nx, ny, N):
+    """Grids above one scan tile (2048 cells) take the three-launch scan whose
+    block sums live in the shared work array; the second case sits exactly at
+    both limits (2^20 particles, 2^20 cells)."""
+    lib = _lib()
+    stream = torch.cuda.Stream()
+    case = _grid_case(nx, ny, N, seed=nx)
+    ref, grid = _reference_celllist(case, "f32")
+    assert grid[:2] == (nx, ny)
+    for _ in range(2):
+        counts, starts, order = _noalloc(lib, case["X0"], "f32", grid, stream)
+        assert np.array_equal(counts, ref["counts"])
+        assert np.array_equal(starts, ref["starts"])
+        assert np.array_equal(order, ref["order"])
 
 
 def test_noalloc_rejects_sizes_beyond_its_limit():
