@@ -576,6 +576,7 @@ def run_ours(args):
     L = S.load()
     stream = torch.cuda.Stream()
     LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
+    S.set_density_tiles(bool(args.density_tiles))
 
     p_d, X0, V0, theta, cfg, interval = select_workload(args)
     p = S.SPHParams(**p_d, dtype=args.dtype)
@@ -858,6 +859,7 @@ def run_ours(args):
                 "recomputed_forward_steps_per_solve": rec,
                 "objective_J": J.value, "kernels_one_solve": kernels,
                 "block_sizes": blocks, "fp64_check": fp64, "graph": graph is not None,
+                "density_form": "cell tiles" if args.density_tiles else "mask walk",
                 "graph_kernels_per_solve": graph.nodes if graph is not None else None}
         print(json.dumps(line))
     if world > 1:
@@ -905,6 +907,9 @@ def main():
                     help="also solve the workload in FP64 on the GPU and report the FP32 "
                          "results' relative difference (the full horizon, and 10 steps of a "
                          "smooth objective); default: on for the single workload")
+    ap.add_argument("--density-tiles", type=int, default=0,
+                    help="density in the cell-tile form (FP32 single states) instead of the "
+                         "per-particle mask walk")
     ap.add_argument("--graph", type=int, default=0,
                     help="time replays of the whole solve captured as one CUDA graph")
     ap.add_argument("--autotune", type=int, default=1,

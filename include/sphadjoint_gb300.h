@@ -235,13 +235,17 @@ SPH_API int32_t sph_batch_objective(sph_workspace ws, sph_state st, int32_t kind
    no tape and no reverse sweep, J alone. Wait for every ticket before
    destroying. */
 typedef struct sph_server_s *sph_server;
+/* snapshots: 0 full tape; c > 0 binomial checkpoints with c snapshots; -1 the
+   server chooses: the full tape when it takes at most an eighth of the HBM
+   budget, else the checkpoint snapshots that fit in that eighth
+   (sph_tape_plan). */
 typedef struct sph_request {
     sph_params p;
     int64_t N;
     const void *X0, *V0;   /* (2, N) T, host */
     const void *theta;     /* (ngy, ngx) column-major T, host */
     int64_t nsteps;
-    int32_t snapshots;     /* 0: full tape; c > 0: binomial checkpoints */
+    int32_t snapshots;     /* 0: full tape; c > 0: binomial checkpoints; -1: chosen */
     int32_t objective;     /* SPH_OBJ_KE_RIGHT or SPH_OBJ_TARGET */
     double obj_args[3];    /* (xc, yc, sigma) for SPH_OBJ_TARGET */
     double skin;
@@ -250,6 +254,18 @@ typedef struct sph_request {
 } sph_request;
 SPH_API int32_t sph_server_create(int32_t workers, int64_t hbm_budget_bytes, int32_t dtype,
                                   sph_server *out);
+/* The packed server: continuous batching at kernel granularity. One scheduler
+   thread admits requests FIFO while their device bytes fit in
+   hbm_budget_bytes and fewer than max_inflight are in flight; every request
+   in flight advances one time step per tick (a forward step, or a reverse
+   step with its recomputation), and each pass of a tick -- the gathers, every
+   cell-list stage, density, forces, pass 1, pass 2, the design-node flush --
+   is one launch over the particles of all of them. A request joins at the
+   next tick after admission and leaves when its solve ends. Results equal the
+   same request solved alone with one thread per particle (bit for bit in
+   FP64). Same submit / wait / poll / stats calls as sph_server_create. */
+SPH_API int32_t sph_server_create_packed(int32_t max_inflight, int64_t hbm_budget_bytes,
+                                         int32_t dtype, sph_server *out);
 SPH_API int32_t sph_server_destroy(sph_server s);
 SPH_API int32_t sph_server_submit(sph_server s, const sph_request *req, int64_t *ticket);
 /* blocks until the request is done; J, latency (submit to done) and flags */
@@ -319,6 +335,14 @@ SPH_API int32_t sph_get_block_sizes(sph_state st, int32_t *blocks);
    forms). Batches always use one thread per particle, so an FP32 batch member
    equals a solo run made with lanes = 1. Other values: SPH_ERR_ARG. */
 SPH_API int32_t sph_set_group_lanes(int32_t lanes);
+/* Density kernel form of FP32 single states that run one thread per particle
+   (no counterpart in the reference), process-wide: 0 (default) walks each
+   particle's neighbour row masks; 1 uses the cell-tile form, where a warp
+   stages the neighbouring cell rows of its 32 consecutive particles in shared
+   memory once and every lane scans all staged candidates. Both add the same
+   terms in the same order; they may differ in the last bits of FP32 through
+   multiply-add contraction. Other values: SPH_ERR_ARG. */
+SPH_API int32_t sph_set_density_tiles(int32_t on);
 SPH_API int32_t sph_get_group_lanes(int32_t *lanes);
 
 /* ---- captured sequences (no counterpart in the reference) ----

@@ -27,6 +27,7 @@ from .api import (  # noqa: F401
     launch_count,
     reset,
     set_group_lanes,
+    set_density_tiles,
     simulate,
     step,
     synchronize,

@@ -103,6 +103,7 @@ _SIGS = {
     "sph_set_block_sizes": (_I32, [_P, _I32P]),
     "sph_get_block_sizes": (_I32, [_P, _I32P]),
     "sph_set_group_lanes": (_I32, [_I32]),
+    "sph_set_density_tiles": (_I32, [_I32]),
     "sph_capture_begin": (_I32, []),
     "sph_capture_end": (_I32, [_PP]),
     "sph_graph_launch": (_I32, [_P]),
@@ -120,6 +121,7 @@ _SIGS = {
     "sph_batch_take_flags": (_I32, [_P, _U32P]),
     "sph_batch_objective": (_I32, [_P, _P, _I32, _DP, _DP]),
     "sph_server_create": (_I32, [_I32, _I64, _I32, _PP]),
+    "sph_server_create_packed": (_I32, [_I32, _I64, _I32, _PP]),
     "sph_server_destroy": (_I32, [_P]),
     "sph_server_submit": (_I32, [_P, C.POINTER(sph_request), _I64P]),
     "sph_server_wait": (_I32, [_P, _I64, _DP, _DP, _U32P]),

@@ -807,6 +807,15 @@ def set_group_lanes(lanes: int) -> None:
     L.check(L.load().sph_set_group_lanes(int(lanes)))
 
 
+def set_density_tiles(on: bool) -> None:
+    """Density kernel form of FP32 single states with one thread per particle
+    (no counterpart in the reference), process-wide: False (default) walks
+    each particle's neighbour masks, True uses the cell-tile form (a warp
+    stages its 32 particles' neighbouring cell rows in shared memory and every
+    lane scans all staged candidates)."""
+    L.check(L.load().sph_set_density_tiles(1 if on else 0))
+
+
 def group_lanes() -> int:
     v = C.c_int32()
     L.check(L.load().sph_get_group_lanes(C.byref(v)))

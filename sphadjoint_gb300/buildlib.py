@@ -28,7 +28,8 @@ SOURCES = {
     "sph_noalloc.cu": ["--fmad=false"],
     "sph_server.cu": [],
 }
-DEPS = ["sph_common.cuh", "sph_kernels.cuh", "sph_coop.cuh", "sph_engine.cuh", "sph_iface.hpp"]
+DEPS = ["sph_common.cuh", "sph_kernels.cuh", "sph_coop.cuh", "sph_engine.cuh", "sph_pack.cuh",
+        "sph_iface.hpp"]
 
 
 def nvcc() -> str:

@@ -24,6 +24,7 @@ thread_local cudaStream_t g_stream = nullptr;
 thread_local bool g_stream_external = false;
 std::atomic<long long> g_launches{0};
 std::atomic<int> g_group_lanes{0};
+std::atomic<bool> g_density_tiles{false};
 thread_local bool g_capturing = false;
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {};
@@ -125,6 +126,8 @@ void rt_sync()
 
 int rt_group_lanes() { return g_group_lanes.load(std::memory_order_relaxed); }
 void rt_set_group_lanes(int lanes) { g_group_lanes.store(lanes, std::memory_order_relaxed); }
+bool rt_density_tiles() { return g_density_tiles.load(std::memory_order_relaxed); }
+void rt_set_density_tiles(bool on) { g_density_tiles.store(on, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
 // Binomial checkpointing (Griewank's revolve bound). With c snapshot slots and
@@ -426,7 +429,7 @@ SPH_API int32_t sph_tape_create_checkpointed(int64_t N, int64_t nsteps, int32_t 
 // in-support masks, densities and staging).
 static int64_t align256(int64_t b) { return (b + 255) & ~(int64_t)255; }
 
-static void tape_sizes(const sph_params *p, int64_t N, int32_t dtype, double skin, int64_t *snap,
+static void tape_sizes(const Params *p, int64_t N, int32_t dtype, double skin, int64_t *snap,
                        int64_t *recomp)
 {
     const int64_t s = dtype == SPH_F64 ? 8 : 4;
@@ -452,9 +455,13 @@ static int64_t device_budget()
     return (int64_t)(0.9 * (double)fr);
 }
 
-static void tape_plan(const sph_params *p, int64_t N, int64_t nsteps, int32_t dtype, double skin,
-                      int64_t budget, int32_t *nsnap, int64_t *bytes)
+} // extern "C"
+
+namespace sphgb {
+void tape_plan(const Params &pr, int64_t N, int64_t nsteps, int dtype, double skin,
+               int64_t budget, int32_t *nsnap, int64_t *bytes)
 {
+    const Params *p = &pr;
     if (N < 0 || nsteps < 0) throw Error(ERR_ARG, "negative tape size");
     const int64_t s = dtype == SPH_F64 ? 8 : 4;
     const int64_t L = std::max<int64_t>(nsteps, 1);
@@ -476,6 +483,9 @@ static void tape_plan(const sph_params *p, int64_t N, int64_t nsteps, int32_t dt
     *nsnap = (int32_t)std::min<int64_t>(c, INT32_MAX);
     *bytes = *nsnap * snap + recomp;
 }
+} // namespace sphgb
+
+extern "C" {
 
 SPH_API int32_t sph_tape_plan(const sph_params *p, int64_t N, int64_t nsteps, int32_t dtype,
                               double skin, int64_t budget_bytes, int32_t *nsnapshots,
@@ -486,8 +496,8 @@ SPH_API int32_t sph_tape_plan(const sph_params *p, int64_t N, int64_t nsteps, in
         check_dtype(dtype);
         int32_t c = 0;
         int64_t b = 0;
-        tape_plan(p, N, nsteps, dtype, skin, budget_bytes < 0 ? device_budget() : budget_bytes,
-                  &c, &b);
+        tape_plan(to_params(p), N, nsteps, dtype, skin,
+                  budget_bytes < 0 ? device_budget() : budget_bytes, &c, &b);
         if (nsnapshots) *nsnapshots = c;
         if (bytes) *bytes = b;
     });
@@ -503,8 +513,8 @@ SPH_API int32_t sph_tape_create_auto(const sph_params *p, int64_t N, int64_t nst
         check_dtype(dtype);
         int32_t c = 0;
         int64_t b = 0;
-        tape_plan(p, N, nsteps, dtype, skin, budget_bytes < 0 ? device_budget() : budget_bytes,
-                  &c, &b);
+        tape_plan(to_params(p), N, nsteps, dtype, skin,
+                  budget_bytes < 0 ? device_budget() : budget_bytes, &c, &b);
         TapeI *t = dtype == SPH_F64 ? make_tape_f64(N, nsteps, c) : make_tape_f32(N, nsteps, c);
         *out = reinterpret_cast<sph_tape>(t);
     });
@@ -613,6 +623,14 @@ SPH_API int32_t sph_get_block_sizes(sph_state st, int32_t *blocks)
         int b[6];
         ST(st)->get_blocks(b);
         for (int k = 0; k < 6; ++k) blocks[k] = b[k];
+    });
+}
+
+SPH_API int32_t sph_set_density_tiles(int32_t on)
+{
+    return guarded([&] {
+        if (on != 0 && on != 1) throw Error(ERR_ARG, "density tiles: 0 or 1");
+        rt_set_density_tiles(on == 1);
     });
 }
 

@@ -713,8 +713,7 @@ template <typename T> class Sys final : public StateI {
             SPH_LAUNCH_COOP(K_ACCEL_INTEGRATE, G, ki, N_, v, vel[cur].p, prho.p, rho.p, theta,
                             pos[nxt].p, vel[nxt].p, aO, alO, flags.p, perm.p, tx, tv);
         } else {
-            auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
-            SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rho.p, prho.p, tmask.p);
+            launch_density(v, rho.p, prho.p);
             v.tmask = tmask.p;
             auto ki = B > 1 ? (anyAV ? &k_accel_integrate<T, true, true> : &k_accel_integrate<T, true>)
                             : (anyAV ? &k_accel_integrate<T, false, true> : &k_accel_integrate<T, false>);
@@ -722,6 +721,22 @@ template <typename T> class Sys final : public StateI {
                              theta, pos[nxt].p, vel[nxt].p, aO, alO, flags.p, perm.p, tx, tv);
         }
         cur = nxt;
+    }
+
+    // density_kernel! + eos_kernel! with one thread per particle: the mask
+    // walk, or for FP32 single states optionally the cell-tile form
+    void launch_density(const NLView<T> &v, T *rhoOut, T2<T> *prhoOut)
+    {
+        if (sizeof(T) == 4 && B == 1 && rt_density_tiles()) {
+            const int bs = 32 * kTileWarps;
+            rt_before_launch(K_DENSITY);
+            k_density_tile<T><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, rt_stream()>>>(
+                v, rhoOut, prhoOut, tmask.p);
+            rt_after_launch(K_DENSITY);
+            return;
+        }
+        auto kd = B > 1 ? &k_density_eos<T, true> : &k_density_eos<T, false>;
+        SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rhoOut, prhoOut, tmask.p);
     }
 
     // theta must hold one (ngy, ngx) block per instance, in instance order
@@ -1192,14 +1207,13 @@ template <typename T> class Work final : public WorkI {
             return;
         }
         const bool multi = S.B > 1;
-        auto kd = multi ? &k_density_eos<T, true> : &k_density_eos<T, false>;
         const bool av = S.anyAV;
         auto ka = multi ? (av ? &k_accel_drag_adj<T, true, true> : &k_accel_drag_adj<T, true>)
                         : (av ? &k_accel_drag_adj<T, false, true> : &k_accel_drag_adj<T, false>);
         auto k1 = multi ? (av ? &k_pass1_design<T, true, true> : &k_pass1_design<T, true>)
                         : (av ? &k_pass1_design<T, false, true> : &k_pass1_design<T, false>);
         auto k2 = multi ? &k_pass2_axpy<T, true> : &k_pass2_axpy<T, false>;
-        SPH_LAUNCH_TUNED(K_DENSITY, multi, kd, N_, v, rhoOut, S.prho.p, S.tmask.p);
+        S.launch_density(v, rhoOut, S.prho.p);
         v.tmask = S.tmask.p;
         SPH_LAUNCH_TUNED(K_ACCEL_DRAG, multi, ka, N_, v, vel, S.prho.p, S.rho.p, theta, gX[gcur].p,
                          gV[gcur].p, abar.p, galpha.p, emax.p, parity);
@@ -1264,7 +1278,9 @@ template <typename T> class Work final : public WorkI {
         }
         jOff = nbTot;
         haveDevSeeds = true;
-        if (rt_capturing()) return; // J stays on the device (objective_value)
+        // while capturing, or when the caller takes no J, J stays on the
+        // device (objective_value) and nothing waits
+        if (rt_capturing() || !J) return;
         SPH_CK(cudaMemcpyAsync(Jb.data(), partial.p + nbTot, sizeof(double) * B, cudaMemcpyDeviceToHost, rt_stream()));
         SPH_CK(cudaStreamSynchronize(rt_stream()));
         for (int b = 0; b < B; ++b)

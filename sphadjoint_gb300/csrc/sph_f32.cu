@@ -1,6 +1,6 @@
 // FP32 instantiation of the engine: same kernels, multiply-add contraction on
 // (checked against the FP64 oracle within a relative tolerance).
-#include "sph_engine.cuh"
+#include "sph_pack.cuh"
 
 namespace sphgb {
 
@@ -19,5 +19,6 @@ WorkI *make_work_f32(const std::vector<Params> &p, const std::vector<int64_t> &N
 {
     return new Work<float>(p, N);
 }
+PackI *make_pack_f32() { return new Packer<float>(); }
 
 } // namespace sphgb

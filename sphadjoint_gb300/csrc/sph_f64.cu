@@ -2,7 +2,7 @@
 // product and sum is rounded separately, as in the reference (Julia does not
 // contract a*b+c without @fastmath / @muladd): results match the oracle bit
 // for bit.
-#include "sph_engine.cuh"
+#include "sph_pack.cuh"
 
 namespace sphgb {
 
@@ -21,5 +21,6 @@ WorkI *make_work_f64(const std::vector<Params> &p, const std::vector<int64_t> &N
 {
     return new Work<double>(p, N);
 }
+PackI *make_pack_f64() { return new Packer<double>(); }
 
 } // namespace sphgb

@@ -87,6 +87,10 @@ void rt_check_launch(const char *name);
 // 16 or 32 = groups for every single-instance state.
 int rt_group_lanes();
 void rt_set_group_lanes(int lanes);
+// Density kernel form of FP32 single states with one thread per particle:
+// false = the per-particle mask walk (default), true = the cell-tile form.
+bool rt_density_tiles();
+void rt_set_density_tiles(bool on);
 // True while the calling thread records its library stream into a CUDA graph:
 // host reads and synchronisations are skipped (results stay on the device)
 // and device allocations are refused.
@@ -172,13 +176,53 @@ class WorkI {
     virtual uint32_t take_flags() = 0;
 };
 
+// One request of the packed engine (sph_pack.cuh): its model, initial state,
+// design field, horizon, tape mode (0 full tape, c > 0 checkpoint snapshots),
+// objective and neighbour-list knobs; adjoint = false runs the forward sweep
+// and the objective only. Host pointers must stay valid until add() returns.
+struct PackReq {
+    Params p;
+    int64_t N = 0;
+    const void *X0 = nullptr, *V0 = nullptr, *theta = nullptr;
+    int64_t nsteps = 0;
+    int32_t snapshots = 0;
+    int32_t objective = 0;
+    double obj_args[3] = {0.0, 0.0, 1.0};
+    NLOpts opts{0.2, 4, 64};
+    bool adjoint = true;
+};
+
+// The packed engine: all requests it holds advance one step per tick, each
+// pass of a tick one grouped launch over all of them (see sph_pack.cuh).
+// Used by one host thread, on that thread's library stream.
+class PackI {
+  public:
+    virtual ~PackI() {}
+    // create the request's device objects (allocates; synchronises the stream)
+    virtual int add(const PackReq &r) = 0;
+    // enqueue one tick; returns the number of requests that took a step
+    virtual int tick() = 0;
+    // requests whose programs have completed on the device (block: wait for
+    // the first unfinished one)
+    virtual void reap(std::vector<int> &done, bool block) = 0;
+    virtual int finishing() const = 0;
+    // J, flags and (adjoint requests) gradients of a completed request,
+    // copied on stream cs into host buffers (any may be NULL)
+    virtual void result(int id, cudaStream_t cs, double *J, uint32_t *flags, void *gX, void *gV,
+                        void *gtheta) = 0;
+    virtual void release(int id) = 0;
+    virtual int active() const = 0;
+    virtual int64_t ticks() const = 0;
+};
+
 #define SPH_DECLARE_FACTORIES(SFX)                                                           \
     FieldI *make_field##SFX(const std::vector<int> &ngx, const std::vector<int> &ngy,        \
                             const void *host);                                               \
     TapeI *make_tape##SFX(int64_t N, int64_t cap, int32_t nsnap);                            \
     StateI *make_state##SFX(const std::vector<Params> &p, const std::vector<int64_t> &N,     \
                             const void *X0, const void *V0, NLOpts o);                       \
-    WorkI *make_work##SFX(const std::vector<Params> &p, const std::vector<int64_t> &N);
+    WorkI *make_work##SFX(const std::vector<Params> &p, const std::vector<int64_t> &N);       \
+    PackI *make_pack##SFX();
 
 SPH_DECLARE_FACTORIES(_f32)
 SPH_DECLARE_FACTORIES(_f64)
@@ -191,5 +235,9 @@ int64_t plan_cost(int64_t l, int64_t c);
 int64_t plan_split(int64_t l, int64_t c);
 // Snapshot positions taken while sweeping forward over l steps with c slots.
 std::vector<int64_t> plan_descent(int64_t l, int64_t c);
+// Tape mode of one state under a device-memory budget: *nsnap = 0 for the full
+// tape, else the most checkpoint snapshots that fit (ERR_NOMEM when none does).
+void tape_plan(const Params &p, int64_t N, int64_t nsteps, int dtype, double skin,
+               int64_t budget, int32_t *nsnap, int64_t *bytes);
 
 } // namespace sphgb

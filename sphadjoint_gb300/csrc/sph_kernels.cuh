@@ -335,6 +335,15 @@ __global__ void __launch_bounds__(kRebuildSmallThreads)
 // which is the set the sequential loop keeps. On 1M particles this form runs
 // 1.8x fewer warp instructions with 29 of 32 lanes active (22 when the limit
 // was tested per slot): 56 instead of 93 us per launch.
+template <typename T, typename IT>
+__device__ __forceinline__ void nl_build_one(int64_t N, const IT &I, int bi, int64_t i,
+                                             const T2<T> *__restrict__ pos,
+                                             const int32_t *__restrict__ cellStart,
+                                             uint32_t *__restrict__ center,
+                                             uint32_t *__restrict__ masks,
+                                             int32_t *__restrict__ nbcount,
+                                             uint32_t *__restrict__ flags);
+
 template <typename T, bool MULTI>
 __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restrict__ inst,
                            const uint16_t *__restrict__ pinst, const T2<T> *__restrict__ pos,
@@ -346,6 +355,20 @@ __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restri
     if (i >= N) return;
     const int bi = MULTI ? (int)pinst[i] : 0;
     decltype(auto) I = pick_inst<MULTI>(one, inst, bi);
+    nl_build_one<T>(N, I, bi, i, pos, cellStart, center, masks, nbcount, flags);
+}
+
+// One particle's neighbour rows (the body of k_nl_build); bi selects its
+// instance's flag word.
+template <typename T, typename IT>
+__device__ __forceinline__ void nl_build_one(int64_t N, const IT &I, int bi, int64_t i,
+                                             const T2<T> *__restrict__ pos,
+                                             const int32_t *__restrict__ cellStart,
+                                             uint32_t *__restrict__ center,
+                                             uint32_t *__restrict__ masks,
+                                             int32_t *__restrict__ nbcount,
+                                             uint32_t *__restrict__ flags)
+{
     const int nx = I.nx, ny = I.ny, maxnb = I.maxnb;
     const T rc2 = I.rc2, r2min = I.r2min;
     const T2<T> xi = pos[i];
@@ -633,12 +656,26 @@ __device__ __forceinline__ void density_finish(const IT &I, int64_t i, T acc, T 
 // passes of the step walk only those (same set, same order), skipping the
 // candidates that the reference's own r^2 test would reject.
 template <typename T, bool MULTI>
+__device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *__restrict__ rho,
+                                             T2<T> *__restrict__ prho,
+                                             uint32_t *__restrict__ tmaskOut);
+
+template <typename T, bool MULTI>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
     k_density_eos(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
                   T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
+    density_walk<T, MULTI>(v, i, rho, prho, tmaskOut);
+}
+
+// The per-particle mask walk of k_density_eos (one thread per particle).
+template <typename T, bool MULTI>
+__device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *__restrict__ rho,
+                                             T2<T> *__restrict__ prho,
+                                             uint32_t *__restrict__ tmaskOut)
+{
     decltype(auto) I = load_inst<MULTI>(v, i);
     const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, A = I.p.A;
     const T2<T> xi = v.pos[i];
@@ -697,6 +734,106 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
     } else {
         acc = density_spill_sum<T>(v, I, i, xi, tmaskOut);
     }
+    density_finish<T>(I, i, acc, rho, prho);
+}
+
+// Density in the cell-tile form: an alternative to the per-particle mask
+// walk for FP32 single states, measured against it and kept off by default
+// (sph_set_density_tiles). A warp takes 32 consecutive slots (its tile). When
+// the tile lies in one cell row and no particle in it is spilled, the warp
+// copies once into shared memory the slot ranges of the three neighbouring
+// cell rows that cover all of its lanes' 3 x 3 cells (particles are stored in
+// cell order, so each row's range is contiguous and the copy is coalesced);
+// every lane then visits every staged candidate, broadcast from shared memory
+// to the warp, and keeps those that are set in its own neighbour row masks
+// and inside the support. Staged rows come in ddy order and slot order within
+// a row, so each lane adds its terms in the reference's scan order
+// (src/forward.jl:25-65). Other warps walk their masks as k_density_eos does.
+constexpr int kTileWarps = 4;
+constexpr int kTileStage = 512; // staged candidates per warp (three rows)
+
+template <typename T>
+__global__ void __launch_bounds__(32 * kTileWarps)
+    k_density_tile(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
+                   T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
+{
+    __shared__ T2<T> stage[kTileWarps][kTileStage];
+    const int w = (int)(threadIdx.x >> 5);
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool live = i < v.N;
+    if (!__any_sync(0xffffffffu, live)) return;
+    const Inst<T> &I = v.one;
+    const uint32_t cc = live ? v.center[i] : 0u;
+    const int cx = (int)(cc & 0xffffu);
+    const int cy = (int)((cc >> 16) & 0x7fffu);
+    const int cymin = __reduce_min_sync(0xffffffffu, live ? cy : INT_MAX);
+    const int cymax = __reduce_max_sync(0xffffffffu, live ? cy : INT_MIN);
+    const int cxmin = __reduce_min_sync(0xffffffffu, live ? cx : INT_MAX);
+    const int cxmax = __reduce_max_sync(0xffffffffu, live ? cx : INT_MIN);
+    const bool spilled = __any_sync(0xffffffffu, live && (cc >> 31));
+    // the staged window: rows cy-1..cy+1, cells max(cxmin-1,1)..min(cxmax+1,nx)
+    int sb[3], sn[3];
+    int total = 0;
+    if (cymin == cymax && !spilled) {
+        const int xa = cxmin - 1 > 1 ? cxmin - 1 : 1;
+        const int xb = cxmax + 1 < I.nx ? cxmax + 1 : I.nx;
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            const int jy = cymin + r - 1;
+            sb[r] = 0;
+            sn[r] = 0;
+            if (jy >= 1 && jy <= I.ny) {
+                const int row = I.coff + (jy - 1) * I.nx;
+                sb[r] = v.cellStart[row + xa - 1];
+                sn[r] = v.cellStart[row + xb] - sb[r];
+            }
+            total += sn[r];
+        }
+    }
+    if (cymin != cymax || spilled || total > kTileStage) {
+        if (live) density_walk<T, false>(v, i, rho, prho, tmaskOut);
+        return;
+    }
+    for (int k = (int)(threadIdx.x & 31u); k < total; k += 32) {
+        const int j = k < sn[0] ? sb[0] + k
+                                : (k < sn[0] + sn[1] ? sb[1] + (k - sn[0]) : sb[2] + (k - sn[0] - sn[1]));
+        stage[w][k] = v.pos[j];
+    }
+    __syncwarp();
+    if (!live) return;
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, A = I.p.A;
+    const T2<T> xi = v.pos[i];
+    const int jx0 = cx - 1 > 1 ? cx - 1 : 1;
+    const int row0 = I.coff + (jx0 - 1) + (cy - 2) * I.nx;
+    T acc = (T)0;
+    int k0 = 0;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const uint64_t mr = ((uint64_t)v.masks[(2 * r + 1) * v.N + i] << 32) | v.masks[2 * r * v.N + i];
+        // slot of the lane's first candidate in row r (its mask's bit 0)
+        const int br = mr ? v.cellStart[row0 + r * I.nx] : 0;
+        uint64_t tw = 0ull;
+        for (int k = 0; k < sn[r]; ++k) {
+            const T2<T> xj = stage[w][k0 + k];
+            const int off = sb[r] + k - br;
+            const bool listed = (unsigned)off < 64u && ((mr >> (off & 63)) & 1ull);
+            const T dx = xi.x - xj.x;
+            const T dy = xi.y - xj.y;
+            const T r2 = dx * dx + dy * dy;
+            const bool in = listed && r2 < r2max;
+            tw |= (uint64_t)in << (off & 63);
+            const T q = pair_sqrt(r2) * invh;
+            const T u = in ? (T)1 - (T)0.5 * q : (T)0;
+            const T u2 = u * u;
+            acc += u2 * u2 * ((T)2 * q + (T)1);
+        }
+        k0 += sn[r];
+        if (tmaskOut) {
+            tmaskOut[(int64_t)(2 * r) * v.N + i] = (uint32_t)tw;
+            tmaskOut[(int64_t)(2 * r + 1) * v.N + i] = (uint32_t)(tw >> 32);
+        }
+    }
+    acc = mul_rn(mul_rn(m, A), acc);
     density_finish<T>(I, i, acc, rho, prho);
 }
 
@@ -1050,6 +1187,11 @@ __device__ __forceinline__ void pass2_finish(const IT &I, int b, int64_t i, cons
                                              const int *__restrict__ emax, int parity,
                                              unsigned long long *__restrict__ thetaAcc);
 
+template <typename T, typename IT>
+__device__ __forceinline__ void pass2_sum(const NLView<T> &v, const IT &I, int64_t i,
+                                          const T2<T> &xi, const T *__restrict__ grho, T &gx,
+                                          T &gy);
+
 // adj_pass2_kernel! (src/adjoint.jl:126-156) + _axpy2!(gX, gXs) + the theta
 // write-back of adj_design_kernel! (src/adjoint.jl:177-184), done as an exact
 // deterministic reduction keyed by design node instead of float atomics.
@@ -1065,10 +1207,22 @@ __global__ void __launch_bounds__(kBlock)
     if (i >= v.N) return;
     const int b = MULTI ? inst_of(v, i) : 0;
     decltype(auto) I = load_inst<MULTI>(v, i);
-    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc;
     const T2<T> xi = v.pos[i];
+    T gx, gy;
+    pass2_sum<T>(v, I, i, xi, grho, gx, gy);
+    pass2_finish<T>(I, b, i, xi, gx, gy, gXs, gX, galpha, emax, parity, thetaAcc);
+}
+
+// The pair loop of adj_pass2_kernel! (src/adjoint.jl:126-156).
+template <typename T, typename IT>
+__device__ __forceinline__ void pass2_sum(const NLView<T> &v, const IT &I, int64_t i,
+                                          const T2<T> &xi, const T *__restrict__ grho, T &gx,
+                                          T &gy)
+{
+    const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc;
     const T gri = grho[i];
-    T gx = 0, gy = 0;
+    gx = 0;
+    gy = 0;
     for_each_neighbor<T>(v, I, i, [&](int j) {
         const T2<T> xj = v.pos[j];
         const T dx = xi.x - xj.x;
@@ -1080,7 +1234,6 @@ __global__ void __launch_bounds__(kBlock)
             gy += w * dy;
         }
     });
-    pass2_finish<T>(I, b, i, xi, gx, gy, gXs, gX, galpha, emax, parity, thetaAcc);
 }
 
 // _axpy2!(gX, gXs) and the exact theta write-back of one particle after its

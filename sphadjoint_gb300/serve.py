@@ -1,10 +1,13 @@
-"""Python side of the request server (sph_server_* in the C ABI).
+"""Python side of the request servers (sph_server_* in the C ABI).
 
 A topology-optimisation caller (the reference's scripts/03_optimize.jl runs
 one simulate!/backward! pair per candidate design) submits forward + adjoint
-solves as its line search produces them; the server runs up to `workers` of
-them concurrently on the GPU, admitting each as soon as a worker is free and
-its device memory fits in the HBM budget.
+solves as its line search produces them. The packed server (``packed=True``)
+advances every request in flight one time step per tick and runs each pass of
+a tick as one launch over all of them, admitting requests FIFO while their
+device memory fits in the HBM budget (and fewer than ``max_inflight`` run).
+The stream server (``packed=False``) runs up to ``workers`` whole solves
+concurrently, each on its own CUDA stream.
 """
 from __future__ import annotations
 
@@ -71,18 +74,29 @@ class Ticket:
 
 
 class Server:
-    def __init__(self, workers: int = 4, hbm_budget_bytes: int = 64 << 30, dtype: str = "f32"):
+    def __init__(self, workers: int = 4, hbm_budget_bytes: int = 64 << 30, dtype: str = "f32",
+                 packed: bool = False, max_inflight: int = 256):
         self._L = L.load()
         self.dtype = dtype
+        self.packed = bool(packed)
         h = C.c_void_p()
         code = {"f64": L.SPH_F64, "f32": L.SPH_F32}[dtype]
-        L.check(self._L.sph_server_create(int(workers), int(hbm_budget_bytes), code, C.byref(h)))
+        if self.packed:
+            L.check(self._L.sph_server_create_packed(int(max_inflight), int(hbm_budget_bytes),
+                                                     code, C.byref(h)))
+        else:
+            L.check(self._L.sph_server_create(int(workers), int(hbm_budget_bytes), code,
+                                              C.byref(h)))
         self.h = h
         self.tickets = []
 
     def submit(self, p: SPHParams, X0, V0, theta, nsteps, snapshots=0, objective="ke_right",
                args=None, skin=0.2, interval=4, maxnb=64, adjoint=True) -> Ticket:
-        """Queue one solve. adjoint=False: forward only, the result holds J alone."""
+        """Queue one solve. adjoint=False: forward only, the result holds J alone.
+        snapshots: 0 full tape, c > 0 checkpoints, "auto" (or -1) chosen by the
+        server from its budget."""
+        if snapshots == "auto":
+            snapshots = -1
         if p.dtype != self.dtype:
             raise ValueError("request dtype differs from the server's")
         t = Ticket(self, p, X0, V0, theta, nsteps, snapshots, objective, args, skin, interval,

@@ -1,0 +1,57 @@
+"""Alternative kernel forms against the default ones on the same inputs.
+
+The cell-tile density (a warp stages its 32 particles' neighbouring cell rows
+in shared memory, every lane scans all staged candidates) keeps exactly the
+mask walk's interaction set and summation order, so it must agree with it to
+FP32 rounding (multiply-add contraction may differ between the two kernels);
+on states where tiles span two cell rows or hold spilled particles, those
+warps take the mask walk."""
+import numpy as np
+import pytest
+
+import cases as K
+from runners import linear_seeds, run_gpu
+
+pytestmark = pytest.mark.gpu
+
+S = pytest.importorskip("sphadjoint_gb300")
+
+
+@pytest.fixture
+def one_thread():
+    S.set_group_lanes(1)
+    yield
+    S.set_group_lanes(0)
+    S.set_density_tiles(False)
+
+
+def dense_case():
+    # rows beyond 64 slots (spilled particles) and cells of ~25 particles
+    rng = np.random.default_rng(9)
+    dp = 0.02
+    p = dict(h=3 * dp, m=dp ** 2, rho0=1.0, c=10.0, mu=0.02, dt=1e-4, Lx=1.0, Ly=0.6,
+             kw=1e4, ngx=9, ngy=7)
+    X0 = K.lattice_block(14, 12, dp, dp, dp, 0.1 * dp, rng)
+    return dict(p=p, X0=X0, V0=0.05 * rng.standard_normal(X0.shape), theta=np.ones((7, 9)))
+
+
+CASES = {
+    "jittered-128": (lambda: K.jittered_block_case(128, ntheta=32), 20),
+    "dambreak": (lambda: K.dambreak_case(theta_seed=4, jitter=0.05), 40),
+    "dense": (dense_case, 8),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_density_tiles_match_the_mask_walk(one_thread, name):
+    make, n = CASES[name]
+    case = make()
+    rng = np.random.default_rng(3)
+    case["cX"] = rng.standard_normal(case["X0"].shape)
+    case["cV"] = rng.standard_normal(case["X0"].shape)
+    out = {}
+    for tiles in (False, True):
+        S.set_density_tiles(tiles)
+        out[tiles] = run_gpu(case, n, dtype="f32", seeds=linear_seeds(case))
+    for k in ("X", "V", "gX", "gV", "gtheta"):
+        assert K.relerr(out[True][k], out[False][k]) <= 1e-5, k
