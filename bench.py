@@ -321,60 +321,124 @@ def served_requests(R, rate, seed=4, ntheta=128, n_range=(2000, 200000),
     return reqs
 
 
-def run_served(args):
-    """Poisson request stream through the continuous-batching server vs the
-    same stream served one request at a time (one worker)."""
+def served_sweep(args):
+    """Poisson streams of forward + adjoint requests (the configuration's
+    topology-optimisation line search) through the packed server, against the
+    same requests served one at a time.
+
+    served: the packed server (every request in flight advances one step per
+    tick, each pass one launch over all of them), admitting requests FIFO by
+    HBM bytes; each rate's stream replayed in real time, latency = submit to
+    done. plain: the requests solved one at a time through the one-worker
+    stream server (the solve-per-call path), submitted back to back so each
+    service time is measured on the GPU; each rate's latencies are the FIFO
+    replay of those service times against that rate's arrival times (one at a
+    time, a request's solve does not depend on when it arrives). Both use the
+    same tape per request: the full tape when it takes at most an eighth of
+    the HBM budget, else the checkpoint snapshots that fit there."""
     import torch
     import sphadjoint_gb300 as S
     from sphadjoint_gb300.serve import Server
 
-    torch.cuda.set_device(0)
     S.load()
-    out = {}
     rates = [float(r) for r in args.rates.split(",")]
-    for mode, workers in (("served", args.workers), ("plain", 1)):
-        res = []
-        for rate in rates:
-            reqs = served_requests(args.requests, rate)
-            with Server(workers=workers, hbm_budget_bytes=int(args.hbm_budget_gb * (1 << 30)),
-                        dtype=args.dtype) as srv:
-                # warm the allocator pool and the code paths
-                w = served_requests(2, 1000.0, seed=99, n_range=(2000, 4000),
-                                    steps_range=(50, 60))
-                for q in w:
-                    srv.submit(S.SPHParams(**q["p"], dtype=args.dtype), q["X0"], q["V0"],
-                               q["theta"], q["steps"], snapshots=q["snapshots"]).wait()
-                srv.reset_stats()
-                srv.tickets.clear()
-                t0 = time.perf_counter()
-                tickets = []
-                for q in reqs:
-                    delay = q["t"] - (time.perf_counter() - t0)
-                    if delay > 0:
-                        time.sleep(delay)
-                    tickets.append(srv.submit(S.SPHParams(**q["p"], dtype=args.dtype), q["X0"],
-                                              q["V0"], q["theta"], q["steps"],
-                                              snapshots=q["snapshots"]))
-                for tk in tickets:
-                    tk.wait()
-                st = srv.stats()
-            ps = sum(q["X0"].shape[1] * q["steps"] for q in reqs)
-            res.append({"rate_per_s": rate, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
-                        "particle_steps_per_s": st["particle_steps_per_s"],
-                        "completed": st["completed"], "peak_inflight": st["peak_inflight"],
-                        "peak_admitted_gb": st["peak_bytes"] / (1 << 30),
-                        "particle_steps": ps})
-        out[mode] = res
-    cfg = {"workload": "served topology-optimisation line search: Poisson arrivals, N uniform "
-                       "in [2k, 200k], steps uniform in [500, 5000], theta = base 128x128 + "
-                       "log-uniform step along a fixed direction, 32 checkpoints per request",
-           "requests_per_rate": args.requests, "rates": rates, "workers": args.workers,
-           "hbm_budget_gb": args.hbm_budget_gb}
+    budget = int(args.hbm_budget_gb * (1 << 30))
+    base = served_requests(args.requests, rates[0])
+    P = [S.SPHParams(**q["p"], dtype=args.dtype) for q in base]
+    snaps = [S.tape_plan(q["X0"].shape[1], q["steps"], p, budget // 8)[0]
+             for q, p in zip(base, P)]
+    ps_req = [q["X0"].shape[1] * q["steps"] for q in base]
+
+    def warm(srv):
+        w = served_requests(2, 1000.0, seed=99, n_range=(2000, 4000), steps_range=(50, 60))
+        for q in w:
+            srv.submit(S.SPHParams(**q["p"], dtype=args.dtype), q["X0"], q["V0"], q["theta"],
+                       q["steps"], snapshots=0).wait()
+        srv.reset_stats()
+        srv.tickets.clear()
+
+    def pct(a, f):
+        a = sorted(a)
+        k = f * (len(a) - 1)
+        i = int(k)
+        j = min(i + 1, len(a) - 1)
+        return a[i] + (a[j] - a[i]) * (k - i)
+
+    served = []
+    for rate in rates:
+        reqs = served_requests(args.requests, rate)
+        with Server(hbm_budget_bytes=budget, dtype=args.dtype, packed=True,
+                    max_inflight=args.max_inflight) as srv:
+            warm(srv)
+            t0 = time.perf_counter()
+            tickets = []
+            for q, p, c in zip(reqs, P, snaps):
+                delay = q["t"] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                tickets.append(srv.submit(p, q["X0"], q["V0"], q["theta"], q["steps"],
+                                          snapshots=c))
+            for tk in tickets:
+                tk.wait()
+            st = srv.stats()
+        served.append({"rate_per_s": rate, "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                       "particle_steps_per_s": st["particle_steps_per_s"],
+                       "completed": st["completed"], "peak_inflight": st["peak_inflight"],
+                       "peak_admitted_gb": st["peak_bytes"] / (1 << 30)})
+
+    # plain: the same requests one at a time, back to back
+    with Server(workers=1, hbm_budget_bytes=budget, dtype=args.dtype) as srv:
+        warm(srv)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        done = []
+        tickets = [srv.submit(p, q["X0"], q["V0"], q["theta"], q["steps"], snapshots=c)
+                   for q, p, c in zip(base, P, snaps)]
+        for tk in tickets:
+            tk.wait()
+            done.append(time.perf_counter() - t0)
+    service = [done[0]] + [done[k] - done[k - 1] for k in range(1, len(done))]
+    plain = []
+    for rate in rates:
+        reqs = served_requests(args.requests, rate)
+        free, lat = 0.0, []
+        for q, sv in zip(reqs, service):
+            start = max(q["t"], free)
+            free = start + sv
+            lat.append(1000.0 * (free - q["t"]))
+        span = free - reqs[0]["t"]
+        plain.append({"rate_per_s": rate, "p50_ms": pct(lat, 0.5), "p99_ms": pct(lat, 0.99),
+                      "particle_steps_per_s": sum(ps_req) / span,
+                      "completed": len(lat)})
+    for a, b in zip(served, plain):
+        a["vs_plain"] = a["particle_steps_per_s"] / b["particle_steps_per_s"]
+    return {"workload": "served topology-optimisation line search: Poisson arrivals at each "
+                        "rate, N uniform in [2k, 200k], steps uniform in [500, 5000], theta = "
+                        "base 128x128 + log-uniform step along a fixed direction",
+            "requests_per_rate": args.requests, "rates": rates,
+            "hbm_budget_gb": args.hbm_budget_gb,
+            "tape": "full tape when it takes at most 1/8 of the budget, else the snapshots "
+                    "that fit there",
+            "full_tape_requests": sum(1 for c in snaps if c == 0),
+            "particle_steps_per_rate": sum(ps_req),
+            "served": served, "plain": plain,
+            "plain_method": "service times measured one at a time back to back; latencies are "
+                            "their FIFO replay against each rate's arrival times",
+            "plain_total_s": done[-1],
+            "vs_plain_min": min(a["vs_plain"] for a in served)}
+
+
+def run_served(args):
+    """--workload served: the served sweep alone, as its own JSON line."""
+    import torch
+
+    torch.cuda.set_device(0)
+    out = served_sweep(args)
     best = max(out["served"], key=lambda r: r["particle_steps_per_s"])
     line = {"metric": "served fwd+adjoint particle-steps/s and p50/p99 latency vs plain",
             "value": best["particle_steps_per_s"], "unit": "particle-steps/s", "n_gpus": 1,
-            "higher_is_better": True, "dtype": args.dtype, "data": "synthetic", "config": cfg,
-            "served": out["served"], "plain": out["plain"]}
+            "higher_is_better": True, "dtype": args.dtype, "data": "synthetic",
+            "config": {"workload": out["workload"]}, "served": out}
     print(json.dumps(line))
 
 
@@ -576,7 +640,7 @@ def run_ours(args):
     L = S.load()
     stream = torch.cuda.Stream()
     LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
-    S.set_density_tiles(bool(args.density_tiles))
+    S.set_density_form(args.density_form)
 
     p_d, X0, V0, theta, cfg, interval = select_workload(args)
     p = S.SPHParams(**p_d, dtype=args.dtype)
@@ -841,6 +905,10 @@ def run_ours(args):
                "ms_per_step": 1000 * te, "steps": args.e2e_steps,
                "pinned_host_buffers": pinned_ok[0]}
 
+    served = None
+    if rank == 0 and world == 1 and args.served and args.workload == "single":
+        served = served_sweep(args)
+
     cpu = None
     if rank == 0 and world == 1 and args.cpu_seconds > 0:
         max_steps = args.nsteps if args.workload == "small" else 64
@@ -859,7 +927,8 @@ def run_ours(args):
                 "recomputed_forward_steps_per_solve": rec,
                 "objective_J": J.value, "kernels_one_solve": kernels,
                 "block_sizes": blocks, "fp64_check": fp64, "graph": graph is not None,
-                "density_form": "cell tiles" if args.density_tiles else "mask walk",
+                "density_form": args.density_form,
+                "served": served,
                 "graph_kernels_per_solve": graph.nodes if graph is not None else None}
         print(json.dumps(line))
     if world > 1:
@@ -874,10 +943,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="single",
                     choices=["single", "small", "dense", "batched", "served"])
-    ap.add_argument("--requests", type=int, default=24, help="served: requests per rate")
+    ap.add_argument("--served", type=int, default=1,
+                    help="single workload: add the served sweep (packed server vs plain) to the "
+                         "line")
+    ap.add_argument("--requests", type=int, default=100, help="served: requests per rate")
     ap.add_argument("--rates", default="10,100,500", help="served: arrival rates (1/s)")
-    ap.add_argument("--workers", type=int, default=12, help="served: concurrent requests")
-    ap.add_argument("--hbm-budget-gb", type=float, default=96.0, help="served: admission budget")
+    ap.add_argument("--max-inflight", type=int, default=256,
+                    help="served: most requests in flight in the packed server")
+    ap.add_argument("--hbm-budget-gb", type=float, default=160.0,
+                    help="served: admission budget")
     ap.add_argument("--instances", type=int, default=64, help="batched: number of instances")
     ap.add_argument("--model", default="reference", choices=sorted(MODELS),
                     help="physics: the reference's (linear EOS, Morris viscosity) or Tait + "
@@ -907,9 +981,9 @@ def main():
                     help="also solve the workload in FP64 on the GPU and report the FP32 "
                          "results' relative difference (the full horizon, and 10 steps of a "
                          "smooth objective); default: on for the single workload")
-    ap.add_argument("--density-tiles", type=int, default=0,
-                    help="density in the cell-tile form (FP32 single states) instead of the "
-                         "per-particle mask walk")
+    ap.add_argument("--density-form", default="pairs", choices=["mask", "tiles", "pairs"],
+                    help="FP32 density kernel form: the per-particle mask walk, the cell-tile "
+                         "form, or the mask walk with two candidates per iteration (f32x2)")
     ap.add_argument("--graph", type=int, default=0,
                     help="time replays of the whole solve captured as one CUDA graph")
     ap.add_argument("--autotune", type=int, default=1,

@@ -27,7 +27,8 @@ from .api import (  # noqa: F401
     launch_count,
     reset,
     set_group_lanes,
-    set_density_tiles,
+    set_density_form,
+    density_form,
     simulate,
     step,
     synchronize,

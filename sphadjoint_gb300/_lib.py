@@ -103,7 +103,8 @@ _SIGS = {
     "sph_set_block_sizes": (_I32, [_P, _I32P]),
     "sph_get_block_sizes": (_I32, [_P, _I32P]),
     "sph_set_group_lanes": (_I32, [_I32]),
-    "sph_set_density_tiles": (_I32, [_I32]),
+    "sph_set_density_form": (_I32, [_I32]),
+    "sph_get_density_form": (_I32, [_I32P]),
     "sph_capture_begin": (_I32, []),
     "sph_capture_end": (_I32, [_PP]),
     "sph_graph_launch": (_I32, [_P]),
@@ -135,6 +136,15 @@ _SIGS = {
     "sph_profile_reset": (_I32, []),
     "sph_plan_cost": (_I64, [_I64, _I64]),
     "sph_plan_split": (_I64, [_I64, _I64]),
+    "sph_design_create": (_I32, [_I32, _I32, _I32, C.c_double, C.c_double, C.c_double, _PP]),
+    "sph_design_destroy": (_I32, [_P]),
+    "sph_design_set": (_I32, [_P, _P]),
+    "sph_design_get": (_I32, [_P, _P, _P, _P]),
+    "sph_design_to_theta": (_I32, [_P, _P]),
+    "sph_design_gradient": (_I32, [_P, _P, _DP]),
+    "sph_design_candidate": (_I32, [_P, C.c_double, _P]),
+    "sph_design_accept": (_I32, [_P]),
+    "sph_design_apply": (_I32, [_P, _I32, _P, _P]),
     "sph_build_cells_noalloc": (_I32, [_P, _I64, _I32, C.c_double, _I32, _I32, _I32P, _I32P,
                                        _I32P, _P]),
 }

@@ -807,13 +807,25 @@ def set_group_lanes(lanes: int) -> None:
     L.check(L.load().sph_set_group_lanes(int(lanes)))
 
 
-def set_density_tiles(on: bool) -> None:
-    """Density kernel form of FP32 single states with one thread per particle
-    (no counterpart in the reference), process-wide: False (default) walks
-    each particle's neighbour masks, True uses the cell-tile form (a warp
-    stages its 32 particles' neighbouring cell rows in shared memory and every
-    lane scans all staged candidates)."""
-    L.check(L.load().sph_set_density_tiles(1 if on else 0))
+DENSITY_FORMS = {"mask": 0, "tiles": 1, "pairs": 2}
+
+
+def set_density_form(form) -> None:
+    """Density kernel form of FP32 states with one thread per particle (no
+    counterpart in the reference), process-wide: "mask" walks each particle's
+    neighbour masks one candidate at a time, "tiles" uses the cell-tile form
+    (a warp stages its 32 particles' neighbouring cell rows in shared memory
+    and every lane scans all staged candidates; single states), "pairs" (the
+    default) walks the masks two candidates per iteration with packed f32x2
+    arithmetic."""
+    L.check(L.load().sph_set_density_form(DENSITY_FORMS[form] if isinstance(form, str)
+                                          else int(form)))
+
+
+def density_form() -> str:
+    v = C.c_int32()
+    L.check(L.load().sph_get_density_form(C.byref(v)))
+    return {c: k for k, c in DENSITY_FORMS.items()}[v.value]
 
 
 def group_lanes() -> int:

@@ -27,6 +27,7 @@ SOURCES = {
     "sph_capi.cu": [],
     "sph_noalloc.cu": ["--fmad=false"],
     "sph_server.cu": [],
+    "sph_design.cu": ["--fmad=false"],
 }
 DEPS = ["sph_common.cuh", "sph_kernels.cuh", "sph_coop.cuh", "sph_engine.cuh", "sph_pack.cuh",
         "sph_iface.hpp"]

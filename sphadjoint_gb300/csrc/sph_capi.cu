@@ -24,7 +24,7 @@ thread_local cudaStream_t g_stream = nullptr;
 thread_local bool g_stream_external = false;
 std::atomic<long long> g_launches{0};
 std::atomic<int> g_group_lanes{0};
-std::atomic<bool> g_density_tiles{false};
+std::atomic<int> g_density_form{2};
 thread_local bool g_capturing = false;
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {};
@@ -126,8 +126,8 @@ void rt_sync()
 
 int rt_group_lanes() { return g_group_lanes.load(std::memory_order_relaxed); }
 void rt_set_group_lanes(int lanes) { g_group_lanes.store(lanes, std::memory_order_relaxed); }
-bool rt_density_tiles() { return g_density_tiles.load(std::memory_order_relaxed); }
-void rt_set_density_tiles(bool on) { g_density_tiles.store(on, std::memory_order_relaxed); }
+int rt_density_form() { return g_density_form.load(std::memory_order_relaxed); }
+void rt_set_density_form(int form) { g_density_form.store(form, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
 // Binomial checkpointing (Griewank's revolve bound). With c snapshot slots and
@@ -626,11 +626,19 @@ SPH_API int32_t sph_get_block_sizes(sph_state st, int32_t *blocks)
     });
 }
 
-SPH_API int32_t sph_set_density_tiles(int32_t on)
+SPH_API int32_t sph_set_density_form(int32_t form)
 {
     return guarded([&] {
-        if (on != 0 && on != 1) throw Error(ERR_ARG, "density tiles: 0 or 1");
-        rt_set_density_tiles(on == 1);
+        if (form < 0 || form > 2) throw Error(ERR_ARG, "density form: 0, 1 or 2");
+        rt_set_density_form(form);
+    });
+}
+
+SPH_API int32_t sph_get_density_form(int32_t *form)
+{
+    return guarded([&] {
+        need(form, "form");
+        *form = rt_density_form();
     });
 }
 

@@ -724,10 +724,16 @@ template <typename T> class Sys final : public StateI {
     }
 
     // density_kernel! + eos_kernel! with one thread per particle: the mask
-    // walk, or for FP32 single states optionally the cell-tile form
+    // walk, or for FP32 states the forms sph_set_density_form selects
     void launch_density(const NLView<T> &v, T *rhoOut, T2<T> *prhoOut)
     {
-        if (sizeof(T) == 4 && B == 1 && rt_density_tiles()) {
+        const int form = sizeof(T) == 4 ? rt_density_form() : 0;
+        if (form == 2) {
+            auto kd = B > 1 ? &k_density_eos<T, true, true> : &k_density_eos<T, false, true>;
+            SPH_LAUNCH_TUNED(K_DENSITY, B > 1, kd, N_, v, rhoOut, prhoOut, tmask.p);
+            return;
+        }
+        if (form == 1 && B == 1) {
             const int bs = 32 * kTileWarps;
             rt_before_launch(K_DENSITY);
             k_density_tile<T><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, rt_stream()>>>(
@@ -1297,6 +1303,13 @@ template <typename T> class Work final : public WorkI {
     }
 
     uint32_t take_flags() override { return lastS ? lastS->take_flags() : 0u; }
+
+    const double *gtheta_device(int64_t n) const override
+    {
+        if (!haveResult) throw Error(ERR_STATE, "no backward pass has run on this workspace");
+        if (n != nnode) throw Error(ERR_ARG, "design size differs from the workspace's theta");
+        return gtheta.p;
+    }
 
     void get(void *gXo, void *gVo, void *gth) override
     {

@@ -87,10 +87,12 @@ void rt_check_launch(const char *name);
 // 16 or 32 = groups for every single-instance state.
 int rt_group_lanes();
 void rt_set_group_lanes(int lanes);
-// Density kernel form of FP32 single states with one thread per particle:
-// false = the per-particle mask walk (default), true = the cell-tile form.
-bool rt_density_tiles();
-void rt_set_density_tiles(bool on);
+// Density kernel form of FP32 states with one thread per particle: 0 = the
+// per-particle mask walk, 1 = the cell-tile form (single states), 2 (default)
+// = the mask walk taking two candidates per iteration in packed f32x2
+// arithmetic.
+int rt_density_form();
+void rt_set_density_form(int form);
 // True while the calling thread records its library stream into a CUDA graph:
 // host reads and synchronisations are skipped (results stay on the device)
 // and device allocations are refused.
@@ -174,6 +176,9 @@ class WorkI {
     virtual void objective_value(double *J) = 0;
     // neighbour-list flags of the last backward's reverse sweep (read and cleared)
     virtual uint32_t take_flags() = 0;
+    // dJ/dtheta of the last backward on the device (double, n nodes; single
+    // instance), for consumers that stay on the device
+    virtual const double *gtheta_device(int64_t n) const = 0;
 };
 
 // One request of the packed engine (sph_pack.cuh): its model, initial state,

@@ -25,6 +25,49 @@ constexpr int kBlock = 256;
 
 __device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
 
+// Two FP32 lanes in one 64-bit register: Blackwell issues mul.rn.f32x2 and
+// fma.rn.f32x2 as one instruction for both halves, each rounded as the scalar
+// operation would be.
+__device__ __forceinline__ float2 fmul2(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+// FP32 pair sums of the reference model (Morris viscosity) in packed form:
+// the x and y components of a pair's differences, force terms and running
+// sums ride in one f32x2 register, so the pair loop issues one instruction
+// where the scalar form issues two; each half rounds as the scalar
+// operation with multiply-add contraction does.
+constexpr bool kPackedPairs = true;
+
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c)
+{
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+        "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+
 // ---------------------------------------------------------------------------
 // Exclusive scan (reduce-then-scan, three launches, no inter-block waits)
 // ---------------------------------------------------------------------------
@@ -655,23 +698,76 @@ __device__ __forceinline__ void density_finish(const IT &I, int64_t i, T acc, T 
 // which neighbour-list entries are inside the support (r^2 < 4h^2): the later
 // passes of the step walk only those (same set, same order), skipping the
 // candidates that the reference's own r^2 test would reject.
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool PAIRS = false>
 __device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *__restrict__ rho,
                                              T2<T> *__restrict__ prho,
                                              uint32_t *__restrict__ tmaskOut);
 
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool PAIRS = false>
 __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
     k_density_eos(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
                   T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
-    density_walk<T, MULTI>(v, i, rho, prho, tmaskOut);
+    density_walk<T, MULTI, PAIRS>(v, i, rho, prho, tmaskOut);
+}
+
+// FP32 density sum over the mask words, two candidates per iteration: both
+// candidates' kernel arithmetic runs in packed f32x2 instructions (each half
+// rounded as the scalar form rounds it) and their terms are added to the one
+// running sum in slot order, so the sum equals the one-candidate loop's. A
+// lone last candidate of a word is paired with itself and adds +0.
+__device__ __forceinline__ float density_pairs_f32(const NLView<float> &v, int64_t i,
+                                                   const float2 &xi, float r2max, float invh,
+                                                   uint64_t m0, uint64_t m1, uint64_t m2, int b0,
+                                                   int b1, int b2,
+                                                   uint32_t *__restrict__ tmaskOut)
+{
+    const float2 ih2 = make_float2(invh, invh), mh = make_float2(-0.5f, -0.5f);
+    const float2 one2 = make_float2(1.0f, 1.0f), two2 = make_float2(2.0f, 2.0f);
+    float acc = 0.0f;
+    uint32_t mw = (uint32_t)m0, tw = 0u;
+    int base = b0;
+    int w = 0;
+    for (;;) {
+        if (mw == 0u) {
+            if (tmaskOut) tmaskOut[(int64_t)w * v.N + i] = tw; // word w is finished
+            tw = 0u;
+            if (++w == 6) break;
+            const uint64_t mr = w < 2 ? m0 : (w < 4 ? m1 : m2);
+            const int br = w < 2 ? b0 : (w < 4 ? b1 : b2);
+            mw = (w & 1) ? (uint32_t)(mr >> 32) : (uint32_t)mr;
+            base = br + ((w & 1) << 5);
+            continue;
+        }
+        const int ka = __ffs((int)mw) - 1;
+        mw &= mw - 1u;
+        const bool two = mw != 0u;
+        const int kb = two ? __ffs((int)mw) - 1 : ka;
+        mw &= two ? mw - 1u : mw;
+        const float2 da = fsub2(xi, v.pos[base + ka]);
+        const float2 db = fsub2(xi, v.pos[base + kb]);
+        const float r2a = da.x * da.x + da.y * da.y;
+        const float r2b = db.x * db.x + db.y * db.y;
+        const bool ina = r2a < r2max;
+        const bool inb = two && r2b < r2max;
+        tw |= ((uint32_t)ina << ka) | ((uint32_t)inb << kb);
+        const float2 q = fmul2(make_float2(pair_sqrt(r2a), pair_sqrt(r2b)), ih2);
+        float2 u = ffma2(q, mh, one2); // 1 - q/2
+        u.x = ina ? u.x : 0.0f;
+        u.y = inb ? u.y : 0.0f;
+        const float2 u2 = fmul2(u, u);
+        const float2 u4 = fmul2(u2, u2);
+        const float2 t = ffma2(q, two2, one2); // 2q + 1
+        acc = fmaf(u4.x, t.x, acc);
+        acc = fmaf(u4.y, t.y, acc);
+    }
+    return acc;
 }
 
 // The per-particle mask walk of k_density_eos (one thread per particle).
-template <typename T, bool MULTI>
+template <typename T, bool MULTI, bool PAIRS>
 __device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *__restrict__ rho,
                                              T2<T> *__restrict__ prho,
                                              uint32_t *__restrict__ tmaskOut)
@@ -693,6 +789,12 @@ __device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *_
         const int b0 = m0 ? v.cellStart[row0] : 0;
         const int b1 = m1 ? v.cellStart[row0 + I.nx] : 0;
         const int b2 = m2 ? v.cellStart[row0 + 2 * I.nx] : 0;
+        if constexpr (PAIRS && sizeof(T) == 4) {
+            acc = density_pairs_f32(v, i, xi, r2max, invh, m0, m1, m2, b0, b1, b2, tmaskOut);
+            acc = mul_rn(mul_rn(m, A), acc);
+            density_finish<T>(I, i, acc, rho, prho);
+            return;
+        }
         uint32_t mw = (uint32_t)m0, tw = 0u;
         int base = b0;
         int w = 0;
@@ -739,7 +841,7 @@ __device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *_
 
 // Density in the cell-tile form: an alternative to the per-particle mask
 // walk for FP32 single states, measured against it and kept off by default
-// (sph_set_density_tiles). A warp takes 32 consecutive slots (its tile). When
+// (sph_set_density_form 1). A warp takes 32 consecutive slots (its tile). When
 // the tile lies in one cell row and no particle in it is spilled, the warp
 // copies once into shared memory the slot ranges of the three neighbouring
 // cell rows that cover all of its lanes' 3 x 3 cells (particles are stored in
@@ -849,6 +951,28 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
     const Visc<T> vc = visc_of<T>(I);
     const T2<T> pi = prho[i];
     const T pti = pi.x, iri = pi.y;
+    if constexpr (sizeof(T) == 4 && !AV && kPackedPairs) {
+        // a_i -= (P_ij F) d, a_i += C (v_i - v_j), both components at once
+        const float tmm = vc.twomumass;
+        float2 acc = make_float2(0.0f, 0.0f);
+        for_each_neighbor<T>(v, I, i, [&](int j) {
+            const float2 d = fsub2(xi, v.pos[j]);
+            const float r2 = d.x * d.x + d.y * d.y;
+            if (r2 < r2max) {
+                const float2 pj = prho[j];
+                const float q = pair_sqrt(r2) * invh;
+                const float u = 1.0f - 0.5f * q;
+                const float F = Fc * u * u * u;
+                const float PF = m * (pti + pj.x) * F;
+                const float C = tmm * iri * pj.y * F;
+                acc = ffma2(make_float2(-PF, -PF), d, acc);
+                acc = ffma2(make_float2(C, C), fsub2(vi, vel[j]), acc);
+            }
+        });
+        ax = acc.x;
+        ay = acc.y;
+        return;
+    }
     const T rhoi = (AV && vc.kind == 1) ? rho[i] : (T)0;
     ax = (T)0;
     ay = (T)0;
@@ -1103,6 +1227,47 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
     const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc, Gc = I.p.Gc;
     const Visc<T> vc = visc_of<T>(I);
     const T pti = pi.x, iri = pi.y;
+    if constexpr (sizeof(T) == 4 && !AV && kPackedPairs) {
+        // the Morris-model pair of adj_pass1_kernel! with (x, y) packed:
+        // g -= (P F) da, g += w d, gv += C da
+        const float tmm = vc.twomumass;
+        float2 g = make_float2(0.0f, 0.0f), gv = make_float2(0.0f, 0.0f);
+        float gr = 0.0f, sS = 0.0f;
+        for_each_neighbor<T>(v, I, i, [&](int j) {
+            const float2 d = fsub2(xi, v.pos[j]);
+            const float r2 = d.x * d.x + d.y * d.y;
+            if (r2 < r2max) {
+                const float2 pj = prho[j];
+                const float rinv = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
+                const float r = r2 * rinv;
+                const float q = r * invh;
+                const float u = 1.0f - 0.5f * q;
+                const float F = Fc * u * u * u;
+                const float G = Gc * u * u;
+                const float PF = m * (pti + pj.x) * F;
+                const float Cbase = tmm * iri * pj.y;
+                const float C = Cbase * F;
+                const float2 da = fsub2(ab, abar[j]);
+                const float2 dv = fsub2(vi, vel[j]);
+                const float ad_d = -(da.x * d.x + da.y * d.y);
+                const float ad_v = da.x * dv.x + da.y * dv.y;
+                const float Fbar = m * (pti + pj.x) * ad_d + Cbase * ad_v;
+                const float w = Fbar * G * invh * rinv;
+                g = ffma2(make_float2(-PF, -PF), da, g);
+                g = ffma2(make_float2(w, w), d, g);
+                gv = ffma2(make_float2(C, C), da, gv);
+                gr -= C * ad_v * iri;
+                sS += F * ad_d;
+            }
+        });
+        gx = g.x;
+        gy = g.y;
+        gvx = gv.x;
+        gvy = gv.y;
+        grh = gr;
+        sumS = sS;
+        return;
+    }
     const T rhoi = (AV && vc.kind == 1) ? rho[i] : (T)0;
     gx = 0, gy = 0, gvx = 0, gvy = 0, grh = 0, sumS = 0;
     for_each_neighbor<T>(v, I, i, [&](int j) {
@@ -1221,6 +1386,20 @@ __device__ __forceinline__ void pass2_sum(const NLView<T> &v, const IT &I, int64
 {
     const T r2max = I.p.r2max, invh = I.p.invh, m = I.p.m, Fc = I.p.Fc;
     const T gri = grho[i];
+    if constexpr (sizeof(T) == 4 && kPackedPairs) {
+        float2 acc = make_float2(0.0f, 0.0f);
+        for_each_neighbor<T>(v, I, i, [&](int j) {
+            const float2 d = fsub2(xi, v.pos[j]);
+            const float r2 = d.x * d.x + d.y * d.y;
+            if (r2 < r2max) {
+                const float w = pass2_weight<float>(r2, invh, m, Fc, gri, grho[j]);
+                acc = ffma2(make_float2(w, w), d, acc);
+            }
+        });
+        gx = acc.x;
+        gy = acc.y;
+        return;
+    }
     gx = 0;
     gy = 0;
     for_each_neighbor<T>(v, I, i, [&](int j) {

@@ -262,8 +262,12 @@ __global__ void __launch_bounds__(kPackBlock) g_nl_build(const GSys<T> *__restri
                     d.flags);
 }
 
+// The pair kernels cap their registers as the tuned single-state kernels do:
+// the request's arrays and constants come from the descriptor table, and
+// holding them all in registers would halve the resident warps.
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_density(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 10 : 1)
+    g_density(const GSys<T> *__restrict__ S, const GList L)
 {
     const int2 f = glist_find(L);
     const GSys<T> &d = S[f.x];
@@ -271,13 +275,14 @@ __global__ void __launch_bounds__(kPackBlock) g_density(const GSys<T> *__restric
     if (i >= d.n) return;
     NLView<T> v = d.v;
     v.tmask = nullptr;
-    density_walk<T, false>(v, i, d.rho, d.prho, d.tmask);
+    density_walk<T, false, true>(v, i, d.rho, d.prho, d.tmask);
 }
 
 // accel_kernel! + integrate_kernel! (forward requests) or the accel
 // recompute + _adj_integrate! + _adj_drag! (reverse requests), per block
 template <typename T, bool AV>
-__global__ void __launch_bounds__(kPackBlock) g_accel(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
+    g_accel(const GSys<T> *__restrict__ S, const GList L)
 {
     const int2 f = glist_find(L);
     const GSys<T> &d = S[f.x];
@@ -285,8 +290,8 @@ __global__ void __launch_bounds__(kPackBlock) g_accel(const GSys<T> *__restrict_
     const bool live = i < d.n;
     if (d.mode == 0) {
         if (!live) return;
-        const NLView<T> v = d.v;
-        const Inst<T> I = v.one;
+        const NLView<T> &v = d.v;
+        const Inst<T> &I = v.one;
         const T2<T> xi = v.pos[i];
         const T2<T> vi = d.vel[i];
         T ax, ay;
@@ -297,8 +302,8 @@ __global__ void __launch_bounds__(kPackBlock) g_accel(const GSys<T> *__restrict_
     }
     int e = INT_MIN;
     if (live) {
-        const NLView<T> v = d.v;
-        const Inst<T> I = v.one;
+        const NLView<T> &v = d.v;
+        const Inst<T> &I = v.one;
         const T2<T> xi = v.pos[i];
         const T2<T> vi = d.vel[i];
         T ax, ay;
@@ -317,15 +322,15 @@ __global__ void __launch_bounds__(kPackBlock) g_accel(const GSys<T> *__restrict_
 }
 
 template <typename T, bool AV>
-__global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
+__global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 9 : 1)
     g_pass1(const GSys<T> *__restrict__ S, const GList L)
 {
     const int2 f = glist_find(L);
     const GSys<T> &d = S[f.x];
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
-    const NLView<T> v = d.v;
-    const Inst<T> I = v.one;
+    const NLView<T> &v = d.v;
+    const Inst<T> &I = v.one;
     const T2<T> xi = v.pos[i];
     const T2<T> vi = d.vel[i];
     const T2<T> ab = d.abar[i];
@@ -339,14 +344,15 @@ __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_pass2(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 12 : 1)
+    g_pass2(const GSys<T> *__restrict__ S, const GList L)
 {
     const int2 f = glist_find(L);
     const GSys<T> &d = S[f.x];
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
-    const NLView<T> v = d.v;
-    const Inst<T> I = v.one;
+    const NLView<T> &v = d.v;
+    const Inst<T> &I = v.one;
     const T2<T> xi = v.pos[i];
     T gx, gy;
     pass2_sum<T>(v, I, i, xi, d.grho, gx, gy);

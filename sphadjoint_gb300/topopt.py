@@ -13,17 +13,25 @@ library's API:
 - the non-discreteness measure Mnd and the CSV outputs (:360-393)
 
 Design variables stay in float64 whatever the particle precision, as in the
-reference (`TW = Float64`). The line search may run its candidate steps
-concurrently on a request Server and still picks exactly the candidate the
-sequential search would (the first improving one).
+reference (`TW = Float64`). By default the design side runs on the device
+(``DeviceDesign``, the library's sph_design_* kernels): the design, its
+filtered field, theta and the gradient never leave the GPU between solves,
+and the line search writes each candidate's theta straight into the solver's
+field. The numpy functions below are the host restatement the device kernels
+are checked against, and the path a request Server takes (it uploads theta per
+request): the line search may run its candidate steps concurrently there and
+still picks exactly the candidate the sequential search would (the first
+improving one).
 """
 from __future__ import annotations
 
+import ctypes as C
 import csv
 from dataclasses import dataclass, field
 
 import numpy as np
 
+from . import _lib as L
 from . import api as S
 
 
@@ -81,6 +89,68 @@ class DensityFilter:
         return out.reshape(self.shape)
 
 
+class DeviceDesign:
+    """The design side of 03_optimize.jl on the device (sph_design_* in the C
+    ABI): alpha(rho), the density filter and its adjoint, the volume
+    projection and the line-search candidate, on a design kept on the GPU.
+    Host arrays are numpy (ngy, ngx)."""
+
+    FILTER, FILTER_ADJOINT, PROJECT, ALPHA, DALPHA = range(5)
+
+    def __init__(self, ngy, ngx, r, alpha_max, qp, volfrac):
+        self._L = L.load()
+        self.shape = (ngy, ngx)
+        h = C.c_void_p()
+        L.check(self._L.sph_design_create(int(ngx), int(ngy), int(r), float(alpha_max),
+                                          float(qp), float(volfrac), C.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self._L.sph_design_destroy(self.h)
+            self.h = None
+
+    def _in(self, x):
+        a = np.asfortranarray(np.asarray(x, dtype=np.float64))
+        if a.shape != self.shape:
+            raise ValueError("design shape differs")
+        return a
+
+    def set(self, rd):
+        a = self._in(rd)
+        L.check(self._L.sph_design_set(self.h, a.ctypes.data_as(C.c_void_p)))
+
+    def get(self):
+        """(rd, filtered rd, gradient) from the device."""
+        out = [np.empty(self.shape, order="F") for _ in range(3)]
+        L.check(self._L.sph_design_get(self.h, *(o.ctypes.data_as(C.c_void_p) for o in out)))
+        return tuple(np.ascontiguousarray(o) for o in out)
+
+    def apply(self, op, x):
+        a = self._in(x)
+        out = np.empty(self.shape, order="F")
+        L.check(self._L.sph_design_apply(self.h, int(op), a.ctypes.data_as(C.c_void_p),
+                                         out.ctypes.data_as(C.c_void_p)))
+        return np.ascontiguousarray(out)
+
+    def to_theta(self, field):
+        L.check(self._L.sph_design_to_theta(self.h, field.h))
+
+    def gradient(self, ws):
+        """grad = filter_adjoint(dJ/dtheta * dalpha(filter(rd))) from the
+        workspace's last backward; returns max |grad|."""
+        g = C.c_double()
+        L.check(self._L.sph_design_gradient(self.h, ws.h, C.byref(g)))
+        return g.value
+
+    def candidate(self, step, field=None):
+        L.check(self._L.sph_design_candidate(self.h, float(step),
+                                             field.h if field is not None else None))
+
+    def accept(self):
+        L.check(self._L.sph_design_accept(self.h))
+
+
 def project_volume(rd, volfrac):
     """Clamp to [0, 1]; if mean < volfrac, shift up by bisection (60 halvings)."""
     x = np.clip(rd, 0.0, 1.0)
@@ -120,12 +190,25 @@ class Problem:
     snapshots: int = 0
 
     use_graphs: bool = True
+    device: bool = True
     filt: DensityFilter = field(init=False)
 
     def __post_init__(self):
         self.filt = DensityFilter(self.p.ngy, self.p.ngx, self.filt_r)
         self.N = int(np.asarray(self.X0).size // 2)
         self._solver = None
+        self._dev = None
+
+    def dev(self) -> DeviceDesign:
+        if self._dev is None:
+            self._dev = DeviceDesign(self.p.ngy, self.p.ngx, self.filt_r, self.alpha_max,
+                                     self.qp, self.volfrac)
+        return self._dev
+
+    def solver(self):
+        if self._solver is None:
+            self._solver = _Solver(self)
+        return self._solver
 
     def theta_of(self, rd):
         return alpha_of(self.filt.apply(rd), self.alpha_max, self.qp)
@@ -134,9 +217,7 @@ class Problem:
         """J (and dJ/dtheta) of one design: objects made once per problem, the
         two solve sequences captured as CUDA graphs on first use and replayed
         with the new design written into the same device field."""
-        if self._solver is None:
-            self._solver = _Solver(self)
-        return self._solver.run(theta, grad)
+        return self.solver().run(theta, grad)
 
     def objective_and_grad(self, rd):
         """J and dJ/drd: filter -> alpha -> simulate -> target_objective ->
@@ -190,7 +271,15 @@ class _Solver:
         S.backward_seeded(self.ws, self.tp, self.th, self.prob.p, interval=self.prob.interval)
 
     def run(self, theta, grad):
+        """J (and dJ/dtheta on the host) for a host theta."""
         self.th.upload(theta)
+        J = self.solve(grad)
+        gt = np.asarray(self.ws.get()[2], np.float64) if grad else None
+        return J, gt
+
+    def solve(self, grad):
+        """One solve of the design the device field holds; returns J (the
+        gradient stays in the workspace)."""
         fn = self._grad if grad else (lambda: self._forward(None))
         if not self.prob.use_graphs:
             fn()
@@ -200,9 +289,7 @@ class _Solver:
         else:
             fn()  # first run allocates; then record it
             self.graphs[grad] = S.capture(fn)
-        J = self.ws.objective_value()
-        gt = np.asarray(self.ws.get()[2], np.float64) if grad else None
-        return J, gt
+        return self.ws.objective_value()
 
 
 def optimize(prob: Problem, rd0=None, maxit=40, step0=0.05, server=None, log=None):
@@ -211,6 +298,8 @@ def optimize(prob: Problem, rd0=None, maxit=40, step0=0.05, server=None, log=Non
     1.3 (capped at 0.3) after an accepted step. With a Server the 6 candidates
     are evaluated concurrently and the first improving one is taken."""
     rd = np.ones((prob.p.ngy, prob.p.ngx)) if rd0 is None else np.array(rd0, np.float64)
+    if prob.device and server is None:
+        return _optimize_device(prob, rd, maxit, step0, log)
     step = float(step0)
     J, g = prob.objective_and_grad(rd)
     hist = [J]
@@ -242,6 +331,44 @@ def optimize(prob: Problem, rd0=None, maxit=40, step0=0.05, server=None, log=Non
         if log:
             log(it, J, float(np.max(np.abs(g))), step, accepted + 1)
     return rd, hist
+
+
+def _optimize_device(prob: Problem, rd, maxit, step0, log):
+    """optimize() with the design on the device: theta of the design and of
+    each candidate is written straight into the solver's field, the gradient
+    is chained from the workspace's dJ/dtheta on the device; only J and
+    max |grad| come back per solve. Same steps, same acceptance rule, same
+    arithmetic as the host path (the filter, its adjoint and alpha(rho) are
+    bit-identical; the projection's means are summed in another order)."""
+    dd, sv = prob.dev(), prob.solver()
+    dd.set(rd)
+    step = float(step0)
+    dd.to_theta(sv.th)
+    J = sv.solve(True)
+    gn = dd.gradient(sv.ws)
+    hist = [J]
+    for it in range(1, maxit + 1):
+        if gn < 1e-30:
+            break
+        steps = [step * 0.5 ** k for k in range(6)]
+        accepted = None
+        for k, s_ in enumerate(steps):
+            dd.candidate(s_, sv.th)
+            Jc = sv.solve(False)
+            if Jc < J:
+                accepted, J = k, Jc
+                break
+        if accepted is None:
+            break
+        dd.accept()
+        step = min(steps[accepted] * 1.3, 0.30)
+        hist.append(J)
+        dd.to_theta(sv.th)
+        sv.solve(True)
+        gn = dd.gradient(sv.ws)
+        if log:
+            log(it, J, gn, step, accepted + 1)
+    return dd.get()[0], hist
 
 
 # ---- outputs (the reference's CSV formats) ---------------------------------

@@ -1,11 +1,12 @@
 """Alternative kernel forms against the default ones on the same inputs.
 
 The cell-tile density (a warp stages its 32 particles' neighbouring cell rows
-in shared memory, every lane scans all staged candidates) keeps exactly the
-mask walk's interaction set and summation order, so it must agree with it to
-FP32 rounding (multiply-add contraction may differ between the two kernels);
-on states where tiles span two cell rows or hold spilled particles, those
-warps take the mask walk."""
+in shared memory, every lane scans all staged candidates) and the two-
+candidate mask walk (packed f32x2 arithmetic) keep exactly the mask walk's
+interaction set and summation order, so they must agree with it to FP32
+rounding (multiply-add contraction may differ between kernels); on states
+where tiles span two cell rows or hold spilled particles, those warps take the
+mask walk."""
 import numpy as np
 import pytest
 
@@ -22,7 +23,7 @@ def one_thread():
     S.set_group_lanes(1)
     yield
     S.set_group_lanes(0)
-    S.set_density_tiles(False)
+    S.set_density_form("pairs")
 
 
 def dense_case():
@@ -42,16 +43,21 @@ CASES = {
 }
 
 
+@pytest.mark.parametrize("form", ["tiles", "pairs"])
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_density_tiles_match_the_mask_walk(one_thread, name):
+def test_density_forms_match_the_mask_walk(one_thread, name, form):
     make, n = CASES[name]
     case = make()
     rng = np.random.default_rng(3)
     case["cX"] = rng.standard_normal(case["X0"].shape)
     case["cV"] = rng.standard_normal(case["X0"].shape)
     out = {}
-    for tiles in (False, True):
-        S.set_density_tiles(tiles)
-        out[tiles] = run_gpu(case, n, dtype="f32", seeds=linear_seeds(case))
+    for f in ("mask", form):
+        S.set_density_form(f)
+        assert S.density_form() == f
+        out[f] = run_gpu(case, n, dtype="f32", seeds=linear_seeds(case))
     for k in ("X", "V", "gX", "gV", "gtheta"):
-        assert K.relerr(out[True][k], out[False][k]) <= 1e-5, k
+        if form == "pairs":  # the same operations in the same order: same bits
+            assert np.array_equal(out[form][k], out["mask"][k]), k
+        else:
+            assert K.relerr(out[form][k], out["mask"][k]) <= 1e-5, k

@@ -34,14 +34,22 @@ def test_optimisation_reaches_published_objective():
     4000 steps, alpha_max 2000): J -48.816 -> -49.685, converged after 2
     iterations (README.md:600-602)."""
     prob = T.reference_problem(dtype="f64")
-    rd_seq, h_seq = T.optimize(prob, maxit=40)
-    assert len(h_seq) == 3
-    assert round(h_seq[0], 3) == -48.816 and round(h_seq[-1], 3) == -49.685
+    rd_dev, h_dev = T.optimize(prob, maxit=40)  # design side on the device
+    assert len(h_dev) == 3
+    assert round(h_dev[0], 3) == -48.816 and round(h_dev[-1], 3) == -49.685
+    assert all(b < a for a, b in zip(h_dev, h_dev[1:]))
+    # the host restatement of the design side takes the same steps
+    host = T.reference_problem(dtype="f64")
+    host.device = False
+    rd_seq, h_seq = T.optimize(host, maxit=40)
+    assert np.max(np.abs(rd_dev - rd_seq)) <= 1e-12
+    assert h_dev == pytest.approx(h_seq, rel=1e-12)
+    # concurrent line-search candidates on a request server: the sequential
+    # host trajectory exactly
     with Server(workers=6, hbm_budget_bytes=16 << 30, dtype="f64") as srv:
-        rd_par, h_par = T.optimize(prob, maxit=40, server=srv)
+        rd_par, h_par = T.optimize(host, maxit=40, server=srv)
     assert np.array_equal(rd_seq, rd_par)
     assert h_seq == pytest.approx(h_par, rel=1e-12)
-    assert all(b < a for a, b in zip(h_seq, h_seq[1:]))
 
 
 def test_forward_only_request_matches_simulate():
