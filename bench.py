@@ -42,19 +42,19 @@ TUNE_STEPS = 32
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 1,048,576
 # particles, FP32 (the --set full captures summarised in profiles/*_1M_fp32.md)
 TRAFFIC_1M_F32 = {
-    "density": 38.239488e6 + 1.775616e6,
-    "accel_integrate": 55.129088e6 + 1.536768e6,
-    "accel_drag": 71.912960e6 + 4.487680e6,
-    "pass1": 76.112128e6 + 4.829952e6,
-    "pass2": 63.410432e6 + 0.497664e6,
+    "density": 38.241536e6 + 0.864512e6,
+    "accel_integrate": 55.135232e6 + 1.583616e6,
+    "accel_drag": 71.916288e6 + 4.792064e6,
+    "pass1": 76.107008e6 + 5.036544e6,
+    "pass2": 63.411712e6 + 0.571136e6,
 }
 
 # smsp__issue_active.avg.pct_of_peak_sustained_active of the same captures:
 # the fraction of cycles in which a warp scheduler issued, the bound these
 # gather kernels actually meet (HBM throughput stays in single digits)
 ISSUE_ACTIVE_1M_F32 = {
-    "density": 0.7828, "accel_integrate": 0.7166, "accel_drag": 0.6977,
-    "pass1": 0.7126, "pass2": 0.7513,
+    "density": 0.7646, "accel_integrate": 0.6868, "accel_drag": 0.6758,
+    "pass1": 0.6788, "pass2": 0.7340,
 }
 
 # algorithmic HBM bytes per particle per launch (compulsory traffic of the
@@ -343,7 +343,13 @@ def served_sweep(args):
     S.load()
     rates = [float(r) for r in args.rates.split(",")]
     budget = int(args.hbm_budget_gb * (1 << 30))
-    base = served_requests(args.requests, rates[0])
+    nr = tuple(int(x) for x in args.served_n.split(","))
+    sr = tuple(int(x) for x in args.served_steps.split(","))
+
+    def served_requests_cfg(R, rate):
+        return served_requests(R, rate, n_range=nr, steps_range=sr)
+
+    base = served_requests_cfg(args.requests, rates[0])
     P = [S.SPHParams(**q["p"], dtype=args.dtype) for q in base]
     snaps = [S.tape_plan(q["X0"].shape[1], q["steps"], p, budget // 8)[0]
              for q, p in zip(base, P)]
@@ -366,7 +372,7 @@ def served_sweep(args):
 
     served = []
     for rate in rates:
-        reqs = served_requests(args.requests, rate)
+        reqs = served_requests_cfg(args.requests, rate)
         with Server(hbm_budget_bytes=budget, dtype=args.dtype, packed=True,
                     max_inflight=args.max_inflight) as srv:
             warm(srv)
@@ -400,7 +406,7 @@ def served_sweep(args):
     service = [done[0]] + [done[k] - done[k - 1] for k in range(1, len(done))]
     plain = []
     for rate in rates:
-        reqs = served_requests(args.requests, rate)
+        reqs = served_requests_cfg(args.requests, rate)
         free, lat = 0.0, []
         for q, sv in zip(reqs, service):
             start = max(q["t"], free)
@@ -948,6 +954,10 @@ def main():
                          "line")
     ap.add_argument("--requests", type=int, default=100, help="served: requests per rate")
     ap.add_argument("--rates", default="10,100,500", help="served: arrival rates (1/s)")
+    ap.add_argument("--served-n", default="2000,200000",
+                    help="served: particle-count range of the requests")
+    ap.add_argument("--served-steps", default="500,5000",
+                    help="served: time-step range of the requests")
     ap.add_argument("--max-inflight", type=int, default=256,
                     help="served: most requests in flight in the packed server")
     ap.add_argument("--hbm-budget-gb", type=float, default=160.0,

@@ -1,5 +1,6 @@
 // FP32 instantiation of the engine: same kernels, multiply-add contraction on
 // (checked against the FP64 oracle within a relative tolerance).
+#define SPH_PACK_T float
 #include "sph_pack.cuh"
 
 namespace sphgb {

@@ -2,6 +2,7 @@
 // product and sum is rounded separately, as in the reference (Julia does not
 // contract a*b+c without @fastmath / @muladd): results match the oracle bit
 // for bit.
+#define SPH_PACK_T double
 #include "sph_pack.cuh"
 
 namespace sphgb {

@@ -27,6 +27,8 @@
 
 #include <deque>
 #include <map>
+#include <string>
+#include <type_traits>
 #include <memory>
 #include <vector>
 
@@ -70,31 +72,56 @@ template <typename T> struct GSys {
     double *gtheta;
 };
 
-// The blocks of one grouped launch: request k owns blocks [start[k], start[k+1]).
-struct GList {
-    const int32_t *sys;
-    const int32_t *start;
-    int32_t cnt;
+// The per-tick table in constant memory: the descriptors of the requests that
+// take a step, and the block lists of the tick's grouped launches (list l:
+// request sys[l][k] owns blocks [start[l][k], start[l][k+1])). A block reads
+// its request's arrays and constants at a block-uniform index, through the
+// constant cache, so they need not be held in registers. One table per
+// translation unit: the includer defines SPH_PACK_T, its precision.
+#ifndef SPH_PACK_T
+#error "define SPH_PACK_T (this translation unit's precision) before including sph_pack.cuh"
+#endif
+constexpr int kMaxPackSys = 64; // requests one tick can hold
+constexpr int kPackLists = 8;
+enum PackList : int {
+    PL_GATHER = 0, PL_CELLS, PL_SCANTOP, PL_SCANTILE, PL_PART, PL_ALL, PL_REV, PL_THETA
 };
+struct PackLists {
+    int32_t cnt[kPackLists];
+    int32_t sys[kPackLists][kMaxPackSys];
+    int32_t start[kPackLists][kMaxPackSys + 1];
+};
+template <typename T> struct PackTable {
+    PackLists L;
+    GSys<T> sys[kMaxPackSys];
+};
+__constant__ PackTable<SPH_PACK_T> c_pack;
 
-__device__ __forceinline__ int2 glist_find(const GList &L)
+template <typename T> __device__ __forceinline__ const GSys<T> &pack_sys(int k)
+{
+    static_assert(std::is_same<T, SPH_PACK_T>::value, "one packed precision per unit");
+    return c_pack.sys[k];
+}
+
+// (request, block within the request) of this block in launch list l
+__device__ __forceinline__ int2 glist_find(int l)
 {
     const int b = (int)blockIdx.x;
-    int lo = 0, hi = L.cnt - 1;
+    int lo = 0, hi = c_pack.L.cnt[l] - 1;
     while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (L.start[mid] <= b) lo = mid;
+        if (c_pack.L.start[l][mid] <= b) lo = mid;
         else hi = mid - 1;
     }
-    return make_int2(L.sys[lo], b - L.start[lo]);
+    return make_int2(c_pack.L.sys[l][lo], b - c_pack.L.start[l][lo]);
 }
 
 // _tape_load! of the reverse step's pre-state into cell order
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_gather(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock) g_gather(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t t = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (t >= d.n) return;
     int32_t s = d.perm[t];
@@ -103,20 +130,20 @@ __global__ void __launch_bounds__(kPackBlock) g_gather(const GSys<T> *__restrict
     d.velPre[t] = d.sv[s];
 }
 
-template <typename T> __global__ void __launch_bounds__(kBlock) g_zero_counts(const GSys<T> *__restrict__ S, const GList L)
+template <typename T> __global__ void __launch_bounds__(kBlock) g_zero_counts(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t c = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (c < d.ncell) d.counts[c] = 0;
 }
 
 // k_assign of one request (single instance, cells from 0)
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_assign(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock) g_assign(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     const bool live = i < d.n;
     int32_t c = -1;
@@ -143,11 +170,11 @@ __global__ void __launch_bounds__(kPackBlock) g_assign(const GSys<T> *__restrict
 
 // exclusive scan of each request's counts: tile sums, per-request scan of the
 // tile sums (one block each), then the tiles with their offsets
-template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_reduce(const GSys<T> *__restrict__ S, const GList L)
+template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_reduce(int l)
 {
     __shared__ int32_t sw[33];
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t base = (int64_t)f.y * kScanTile;
     int32_t s = 0;
 #pragma unroll
@@ -160,11 +187,11 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_reduce(co
     if (threadIdx.x == 0) d.scanTmp[f.y] = tot;
 }
 
-template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_top(const GSys<T> *__restrict__ S, const GList L)
+template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_top(int l)
 {
     __shared__ int32_t sw[33];
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t nb = (d.ncell + kScanTile - 1) / kScanTile;
     int32_t carry = 0;
     for (int64_t base = 0; base < nb; base += blockDim.x) {
@@ -177,12 +204,12 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_top(const
     }
 }
 
-template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_down(const GSys<T> *__restrict__ S, const GList L)
+template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_down(int l)
 {
     __shared__ int32_t sw[33];
     constexpr int IPT = kScanTile / kBlock;
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t n = d.ncell;
     const int64_t base = (int64_t)f.y * kScanTile + (int64_t)threadIdx.x * IPT;
     int32_t v[IPT];
@@ -208,10 +235,10 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_down(cons
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_bucket(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock) g_bucket(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     const bool live = i < d.n;
     const int32_t c = live ? d.cellTmp[i] : -1;
@@ -228,10 +255,10 @@ __global__ void __launch_bounds__(kPackBlock) g_bucket(const GSys<T> *__restrict
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_rank(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock) g_rank(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t s = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (s >= d.n) return;
     const int32_t src = d.bucketSrc[s];
@@ -252,10 +279,10 @@ __global__ void __launch_bounds__(kPackBlock) g_rank(const GSys<T> *__restrict__
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPackBlock) g_nl_build(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kPackBlock) g_nl_build(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     nl_build_one<T>(d.n, d.v.one, 0, i, d.v.pos, d.cellStart, d.center, d.masks, d.nbcount,
@@ -267,10 +294,10 @@ __global__ void __launch_bounds__(kPackBlock) g_nl_build(const GSys<T> *__restri
 // holding them all in registers would halve the resident warps.
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 10 : 1)
-    g_density(const GSys<T> *__restrict__ S, const GList L)
+    g_density(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     NLView<T> v = d.v;
@@ -282,10 +309,10 @@ __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 10 : 1)
 // recompute + _adj_integrate! + _adj_drag! (reverse requests), per block
 template <typename T, bool AV>
 __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
-    g_accel(const GSys<T> *__restrict__ S, const GList L)
+    g_accel(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     const bool live = i < d.n;
     if (d.mode == 0) {
@@ -323,10 +350,10 @@ __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
 
 template <typename T, bool AV>
 __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 9 : 1)
-    g_pass1(const GSys<T> *__restrict__ S, const GList L)
+    g_pass1(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const NLView<T> &v = d.v;
@@ -345,10 +372,10 @@ __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 9 : 1)
 
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 12 : 1)
-    g_pass2(const GSys<T> *__restrict__ S, const GList L)
+    g_pass2(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     if (i >= d.n) return;
     const NLView<T> &v = d.v;
@@ -360,11 +387,11 @@ __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 12 : 1)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBlock) g_theta(const GSys<T> *__restrict__ S, const GList L)
+__global__ void __launch_bounds__(kBlock) g_theta(int l)
 {
-    const int2 f = glist_find(L);
-    const GSys<T> &d = S[f.x];
-    theta_node<T>((int64_t)f.y * blockDim.x + threadIdx.x, d.nnode, 1, &S[f.x].v.one, d.thetaAcc,
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
+    theta_node<T>((int64_t)f.y * blockDim.x + threadIdx.x, d.nnode, 1, &d.v.one, d.thetaAcc,
                   d.emax, d.parity, d.gtheta);
 }
 
@@ -489,11 +516,10 @@ template <typename T> class Packer final : public PackI {
         }
     };
 
-    // one tick's descriptor tables: pinned host staging and device copy
+    // one tick's table, staged in pinned host memory for the asynchronous
+    // copy into the constant table; the event marks when the copy is done
     struct Ring {
         uint8_t *host = nullptr;
-        DevBuf<uint8_t> dev;
-        size_t cap = 0;
         cudaEvent_t ev = nullptr;
         bool used = false;
     };
@@ -610,6 +636,9 @@ template <typename T> class Packer final : public PackI {
         }
         if (parts.empty()) return 0;
         const int P = (int)parts.size();
+        if (P > kMaxPackSys)
+            throw Error(ERR_STATE, "more requests in flight than one tick holds (" +
+                                       std::to_string(kMaxPackSys) + ")");
 
         // descriptors, and the block lists of each grouped launch
         std::vector<GSys<T>> sys((size_t)P);
@@ -728,63 +757,51 @@ template <typename T> class Packer final : public PackI {
             Y.cur = rev ? post : 1 - post;
         }
 
-        // upload: descriptors, then every list's sys/start arrays
+        // upload: the block lists, then the descriptors, into the constant table
         Ring &R = ring_[ringPos_];
         ringPos_ = (ringPos_ + 1) % kRing;
         if (R.used) SPH_CK(cudaEventSynchronize(R.ev));
-        std::vector<List *> lists{&lGather, &lCells, &lScanTop, &lScanTile, &lPart, &lAll, &lRev, &lTheta};
-        size_t bytes = sizeof(GSys<T>) * (size_t)P;
-        bytes = (bytes + 255) & ~(size_t)255;
-        std::vector<size_t> offs;
-        for (List *l : lists) {
-            offs.push_back(bytes);
-            bytes += sizeof(int32_t) * (l->sys.size() + l->start.size());
+        const List *lists[kPackLists] = {&lGather, &lCells, &lScanTop, &lScanTile,
+                                         &lPart, &lAll, &lRev, &lTheta};
+        const size_t bytes = sizeof(PackLists) + sizeof(GSys<T>) * (size_t)P;
+        if (!R.host) {
+            SPH_CK(cudaHostAlloc((void **)&R.host, sizeof(PackTable<T>), cudaHostAllocDefault));
+            SPH_CK(cudaEventCreateWithFlags(&R.ev, cudaEventDisableTiming));
         }
-        if (bytes > R.cap) {
-            if (R.host) SPH_CK(cudaFreeHost(R.host));
-            R.host = nullptr;
-            const size_t cap = std::max<size_t>(bytes * 2, 1 << 16);
-            SPH_CK(cudaHostAlloc((void **)&R.host, cap, cudaHostAllocDefault));
-            R.dev.alloc(cap);
-            R.cap = cap;
-            if (!R.ev) SPH_CK(cudaEventCreateWithFlags(&R.ev, cudaEventDisableTiming));
+        PackTable<T> *tab = reinterpret_cast<PackTable<T> *>(R.host);
+        for (int li = 0; li < kPackLists; ++li) {
+            const List &l = *lists[li];
+            tab->L.cnt[li] = (int32_t)l.sys.size();
+            std::copy(l.sys.begin(), l.sys.end(), tab->L.sys[li]);
+            std::copy(l.start.begin(), l.start.end(), tab->L.start[li]);
         }
-        std::memcpy(R.host, sys.data(), sizeof(GSys<T>) * (size_t)P);
-        std::vector<GList> gl;
-        for (size_t li = 0; li < lists.size(); ++li) {
-            List &l = *lists[li];
-            int32_t *h = (int32_t *)(R.host + offs[li]);
-            std::memcpy(h, l.sys.data(), sizeof(int32_t) * l.sys.size());
-            std::memcpy(h + l.sys.size(), l.start.data(), sizeof(int32_t) * l.start.size());
-            const int32_t *dptr = (const int32_t *)(R.dev.p + offs[li]);
-            gl.push_back(GList{dptr, dptr + l.sys.size(), (int32_t)l.sys.size()});
-        }
+        std::memcpy(tab->sys, sys.data(), sizeof(GSys<T>) * (size_t)P);
         cudaStream_t st = rt_stream();
-        SPH_CK(cudaMemcpyAsync(R.dev.p, R.host, bytes, cudaMemcpyHostToDevice, st));
-        const GSys<T> *ds = (const GSys<T> *)R.dev.p;
-        auto launch = [&](int kid, const List &l, int bs, auto kern, const GList &g) {
+        SPH_CK(cudaMemcpyToSymbolAsync(c_pack, R.host, bytes, 0, cudaMemcpyHostToDevice, st));
+        auto launch = [&](int kid, int li, int bs, auto kern) {
+            const List &l = *lists[li];
             if (l.blocks() <= 0) return;
             rt_before_launch(kid);
-            kern<<<(unsigned)l.blocks(), bs, 0, st>>>(ds, g);
+            kern<<<(unsigned)l.blocks(), bs, 0, st>>>(li);
             rt_after_launch(kid);
             ++launches_;
         };
-        launch(K_GATHER, lGather, kPackBlock, g_gather<T>, gl[0]);
-        launch(K_ASSIGN, lCells, kBlock, g_zero_counts<T>, gl[1]);
-        launch(K_ASSIGN, lPart, kPackBlock, g_assign<T>, gl[4]);
-        launch(K_SCAN, lScanTile, kBlock, g_scan_reduce<T>, gl[3]);
-        launch(K_SCAN, lScanTop, kBlock, g_scan_top<T>, gl[2]);
-        launch(K_SCAN, lScanTile, kBlock, g_scan_down<T>, gl[3]);
-        launch(K_BUCKET, lPart, kPackBlock, g_bucket<T>, gl[4]);
-        launch(K_RANK, lPart, kPackBlock, g_rank<T>, gl[4]);
-        launch(K_NLBUILD, lPart, kPackBlock, g_nl_build<T>, gl[4]);
-        launch(K_DENSITY, lAll, kPackBlock, g_density<T>, gl[5]);
-        if (anyAV) launch(K_ACCEL_DRAG, lAll, kPackBlock, g_accel<T, true>, gl[5]);
-        else launch(K_ACCEL_DRAG, lAll, kPackBlock, g_accel<T, false>, gl[5]);
-        if (anyAV) launch(K_PASS1, lRev, kPackBlock, g_pass1<T, true>, gl[6]);
-        else launch(K_PASS1, lRev, kPackBlock, g_pass1<T, false>, gl[6]);
-        launch(K_PASS2, lRev, kPackBlock, g_pass2<T>, gl[6]);
-        launch(K_THETA_NODE, lTheta, kBlock, g_theta<T>, gl[7]);
+        launch(K_GATHER, PL_GATHER, kPackBlock, g_gather<T>);
+        launch(K_ASSIGN, PL_CELLS, kBlock, g_zero_counts<T>);
+        launch(K_ASSIGN, PL_PART, kPackBlock, g_assign<T>);
+        launch(K_SCAN, PL_SCANTILE, kBlock, g_scan_reduce<T>);
+        launch(K_SCAN, PL_SCANTOP, kBlock, g_scan_top<T>);
+        launch(K_SCAN, PL_SCANTILE, kBlock, g_scan_down<T>);
+        launch(K_BUCKET, PL_PART, kPackBlock, g_bucket<T>);
+        launch(K_RANK, PL_PART, kPackBlock, g_rank<T>);
+        launch(K_NLBUILD, PL_PART, kPackBlock, g_nl_build<T>);
+        launch(K_DENSITY, PL_ALL, kPackBlock, g_density<T>);
+        if (anyAV) launch(K_ACCEL_DRAG, PL_ALL, kPackBlock, g_accel<T, true>);
+        else launch(K_ACCEL_DRAG, PL_ALL, kPackBlock, g_accel<T, false>);
+        if (anyAV) launch(K_PASS1, PL_REV, kPackBlock, g_pass1<T, true>);
+        else launch(K_PASS1, PL_REV, kPackBlock, g_pass1<T, false>);
+        launch(K_PASS2, PL_REV, kPackBlock, g_pass2<T>);
+        launch(K_THETA_NODE, PL_THETA, kBlock, g_theta<T>);
         SPH_CK(cudaEventRecord(R.ev, st));
         R.used = true;
         rt_check_launch("packed tick");

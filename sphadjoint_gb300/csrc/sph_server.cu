@@ -367,7 +367,8 @@ class PackedServer final : public Server {
     PackedServer(int maxInflight, int64_t budget, int dtype) : Server(budget, dtype)
     {
         if (maxInflight < 1) throw Error(ERR_ARG, "need at least one request in flight");
-        maxInflight_ = maxInflight;
+        // the packed engine's per-tick table holds 64 requests
+        maxInflight_ = std::min(maxInflight, 64);
         threads_.emplace_back([this] { run_packed(); });
     }
     ~PackedServer() override { stop(); }
