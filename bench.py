@@ -647,6 +647,7 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     LB.check(L.sph_set_stream(C.c_void_p(stream.cuda_stream)))
     S.set_density_form(args.density_form)
+    S.set_launch_overlap(bool(args.overlap))
 
     p_d, X0, V0, theta, cfg, interval = select_workload(args)
     p = S.SPHParams(**p_d, dtype=args.dtype)
@@ -933,7 +934,7 @@ def run_ours(args):
                 "recomputed_forward_steps_per_solve": rec,
                 "objective_J": J.value, "kernels_one_solve": kernels,
                 "block_sizes": blocks, "fp64_check": fp64, "graph": graph is not None,
-                "density_form": args.density_form,
+                "density_form": args.density_form, "launch_overlap": bool(args.overlap),
                 "served": served,
                 "graph_kernels_per_solve": graph.nodes if graph is not None else None}
         print(json.dumps(line))
@@ -994,6 +995,9 @@ def main():
     ap.add_argument("--density-form", default="pairs", choices=["mask", "tiles", "pairs"],
                     help="FP32 density kernel form: the per-particle mask walk, the cell-tile "
                          "form, or the mask walk with two candidates per iteration (f32x2)")
+    ap.add_argument("--overlap", type=int, default=1,
+                    help="programmatic dependent launch of the engine's kernels (1) or plain "
+                         "stream order (0)")
     ap.add_argument("--graph", type=int, default=0,
                     help="time replays of the whole solve captured as one CUDA graph")
     ap.add_argument("--autotune", type=int, default=1,

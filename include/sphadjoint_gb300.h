@@ -386,6 +386,14 @@ SPH_API int32_t sph_set_group_lanes(int32_t lanes);
    terms in the same order; they may differ in the last bits of FP32 through
    multiply-add contraction. Other values: SPH_ERR_ARG. */
 SPH_API int32_t sph_set_density_form(int32_t form);
+/* Programmatic dependent launch (no counterpart in the reference),
+   process-wide: 1 (default) launches the engine's kernels so that each may be
+   scheduled while its predecessor on the stream still runs, waiting on the
+   device for the predecessor's results; this removes most of the launch gap
+   between the short kernels of small states. 0 launches them one after the
+   other. Results do not depend on it; captured sequences always use plain
+   launches. */
+SPH_API int32_t sph_set_launch_overlap(int32_t on);
 SPH_API int32_t sph_get_density_form(int32_t *form);
 SPH_API int32_t sph_get_group_lanes(int32_t *lanes);
 

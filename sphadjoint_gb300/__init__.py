@@ -28,6 +28,7 @@ from .api import (  # noqa: F401
     reset,
     set_group_lanes,
     set_density_form,
+    set_launch_overlap,
     density_form,
     simulate,
     step,

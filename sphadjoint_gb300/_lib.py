@@ -104,6 +104,7 @@ _SIGS = {
     "sph_get_block_sizes": (_I32, [_P, _I32P]),
     "sph_set_group_lanes": (_I32, [_I32]),
     "sph_set_density_form": (_I32, [_I32]),
+    "sph_set_launch_overlap": (_I32, [_I32]),
     "sph_get_density_form": (_I32, [_I32P]),
     "sph_capture_begin": (_I32, []),
     "sph_capture_end": (_I32, [_PP]),

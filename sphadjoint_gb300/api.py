@@ -822,6 +822,13 @@ def set_density_form(form) -> None:
                                           else int(form)))
 
 
+def set_launch_overlap(on: bool) -> None:
+    """Programmatic dependent launch of the engine's kernels (default on): each
+    kernel may be scheduled while its predecessor still runs and waits on the
+    device for its results. Results do not depend on it."""
+    L.check(L.load().sph_set_launch_overlap(1 if on else 0))
+
+
 def density_form() -> str:
     v = C.c_int32()
     L.check(L.load().sph_get_density_form(C.byref(v)))

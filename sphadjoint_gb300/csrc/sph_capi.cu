@@ -25,6 +25,7 @@ thread_local bool g_stream_external = false;
 std::atomic<long long> g_launches{0};
 std::atomic<int> g_group_lanes{0};
 std::atomic<int> g_density_form{2};
+std::atomic<bool> g_launch_overlap{true};
 thread_local bool g_capturing = false;
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {};
@@ -127,6 +128,8 @@ void rt_sync()
 int rt_group_lanes() { return g_group_lanes.load(std::memory_order_relaxed); }
 void rt_set_group_lanes(int lanes) { g_group_lanes.store(lanes, std::memory_order_relaxed); }
 int rt_density_form() { return g_density_form.load(std::memory_order_relaxed); }
+bool rt_launch_overlap() { return g_launch_overlap.load(std::memory_order_relaxed); }
+void rt_set_launch_overlap(bool on) { g_launch_overlap.store(on, std::memory_order_relaxed); }
 void rt_set_density_form(int form) { g_density_form.store(form, std::memory_order_relaxed); }
 
 // ---------------------------------------------------------------------------
@@ -631,6 +634,14 @@ SPH_API int32_t sph_set_density_form(int32_t form)
     return guarded([&] {
         if (form < 0 || form > 2) throw Error(ERR_ARG, "density form: 0, 1 or 2");
         rt_set_density_form(form);
+    });
+}
+
+SPH_API int32_t sph_set_launch_overlap(int32_t on)
+{
+    return guarded([&] {
+        if (on != 0 && on != 1) throw Error(ERR_ARG, "launch overlap: 0 or 1");
+        rt_set_launch_overlap(on == 1);
     });
 }
 

@@ -27,6 +27,18 @@ template <typename T> __host__ __device__ __forceinline__ T2<T> mk2(T x, T y)
     return r;
 }
 
+// Programmatic dependent launch. A kernel the engine launches with the
+// programmatic-stream-serialisation attribute may be scheduled while its
+// predecessor on the stream still runs: it first lets its own successor be
+// scheduled (once all of its blocks have started), then waits until the
+// predecessor grid has completed and its writes are visible, before touching
+// memory. Successive short kernels then start without the launch gap. Without
+// the attribute both instructions return at once.
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.launch_dependents;\n\tgriddepcontrol.wait;" ::: "memory");
+}
+
 // Products and sums that are never contracted into FMA, whatever the build
 // flags: the neighbour-list predicates must see the same r^2 in every kernel.
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }

@@ -167,6 +167,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                     uint32_t *__restrict__ masks, int32_t *__restrict__ nbcount,
                     uint32_t *__restrict__ flags)
 {
+    pdl_enter();
     const Group<G> g;
     const int64_t i = (int64_t)blockIdx.x * (kCoopBlock / G) + g.gi;
     if (i >= N) return; // the whole group
@@ -230,6 +231,7 @@ __global__ void __launch_bounds__(kCoopBlock)
     k_density_eos_coop(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
                        T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
 {
+    pdl_enter();
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][G];
     __shared__ uint32_t tws[NG][6];
@@ -363,6 +365,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                            uint32_t *__restrict__ flags, const int32_t *__restrict__ perm,
                            T2<T> *__restrict__ tx, T2<T> *__restrict__ tv)
 {
+    pdl_enter();
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][4][G];
     __shared__ int32_t lst[NG][kSpillList];
@@ -397,6 +400,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                           T2<T> *__restrict__ abar, T *__restrict__ galpha,
                           int *__restrict__ emax, int parity)
 {
+    pdl_enter();
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][4][G];
     __shared__ int32_t lst[NG][kSpillList];
@@ -430,6 +434,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                         const T2<T> *__restrict__ abar, const T *__restrict__ galpha,
                         T2<T> *__restrict__ gXs, T *__restrict__ grho, T2<T> *__restrict__ gV)
 {
+    pdl_enter();
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][9][G]; // eight term slots and a row of zeros
     __shared__ int32_t lst[NG][kSpillList];
@@ -525,6 +530,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                       const T *__restrict__ galpha, const int *__restrict__ emax, int parity,
                       unsigned long long *__restrict__ thetaAcc)
 {
+    pdl_enter();
     constexpr int NG = kCoopBlock / G;
     __shared__ T buf[NG][2][G];
     __shared__ int32_t lst[NG][kSpillList];

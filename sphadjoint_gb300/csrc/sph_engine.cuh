@@ -95,6 +95,29 @@ template <typename T> struct DevBuf {
 
 inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
+// Launch on the library stream. Outside graph capture, and unless switched off
+// (sph_set_launch_overlap), kernels go out with programmatic dependent launch:
+// each may be scheduled while its predecessor still runs and waits on the
+// device (pdl_enter) for the predecessor's results, which removes the launch
+// gap between the many short kernels of a step.
+template <typename... KArgs, typename... Args>
+inline void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args &&...args)
+{
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = rt_stream();
+    cudaLaunchAttribute at[1];
+    if (rt_launch_overlap() && !rt_capturing()) {
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+    }
+    cuda_check(cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...), "kernel launch");
+}
+
 // Threads per block of each tuned kernel, per precision and per single/batched
 // variant; 256 until autotune() has measured the candidates on a real state.
 template <typename T> int &tuned_block(int kid, bool multi)
@@ -110,7 +133,7 @@ template <typename T> int &tuned_block(int kid, bool multi)
         if ((n) > 0) {                                                                        \
             const int bs_ = ::sphgb::tuned_block<T>(kid, multi);                              \
             ::sphgb::rt_before_launch(kid);                                                   \
-            kern<<<(unsigned)(((n) + bs_ - 1) / bs_), bs_, 0, ::sphgb::rt_stream()>>>(__VA_ARGS__); \
+            ::sphgb::launch_k(kern, dim3((unsigned)(((n) + bs_ - 1) / bs_)), dim3(bs_), 0, __VA_ARGS__); \
             ::sphgb::rt_after_launch(kid);                                                    \
         }                                                                                     \
     } while (0)
@@ -119,7 +142,7 @@ template <typename T> int &tuned_block(int kid, bool multi)
     do {                                                                                      \
         if ((n) > 0) {                                                                        \
             ::sphgb::rt_before_launch(kid);                                                   \
-            kern<<<::sphgb::grid_for(n), ::sphgb::kBlock, 0, ::sphgb::rt_stream()>>>(__VA_ARGS__); \
+            ::sphgb::launch_k(kern, dim3(::sphgb::grid_for(n)), dim3(::sphgb::kBlock), 0, __VA_ARGS__); \
             ::sphgb::rt_after_launch(kid);                                                    \
         }                                                                                     \
     } while (0)
@@ -131,8 +154,8 @@ template <typename T> int &tuned_block(int kid, bool multi)
         if ((n) > 0) {                                                                        \
             const int per_ = ::sphgb::kCoopBlock / (G);                                       \
             ::sphgb::rt_before_launch(kid);                                                   \
-            kern<<<(unsigned)(((n) + per_ - 1) / per_), ::sphgb::kCoopBlock, 0,               \
-                   ::sphgb::rt_stream()>>>(__VA_ARGS__);                                      \
+            ::sphgb::launch_k(kern, dim3((unsigned)(((n) + per_ - 1) / per_)),                 \
+                              dim3(::sphgb::kCoopBlock), 0, __VA_ARGS__);                       \
             ::sphgb::rt_after_launch(kid);                                                    \
         }                                                                                     \
     } while (0)
@@ -205,14 +228,14 @@ inline void scan_excl(const int32_t *in, int64_t n, int32_t *out, int32_t *out2,
     const int64_t nb = (n + kScanTile - 1) / kScanTile;
     if (nb <= 1) {
         rt_before_launch(K_SCAN);
-        k_scan_down<<<1, kBlock, 0, rt_stream()>>>(in, n, nullptr, out, out2);
+        launch_k(k_scan_down, dim3(1), dim3(kBlock), 0, in, n, (const int32_t *)nullptr, out, out2);
         rt_after_launch(K_SCAN);
         return;
     }
     rt_before_launch(K_SCAN);
-    k_scan_reduce<<<(unsigned)nb, kBlock, 0, rt_stream()>>>(in, n, tmp);
-    k_scan_top<<<1, 1024, 0, rt_stream()>>>(tmp, nb);
-    k_scan_down<<<(unsigned)nb, kBlock, 0, rt_stream()>>>(in, n, tmp, out, out2);
+    launch_k(k_scan_reduce, dim3((unsigned)nb), dim3(kBlock), 0, in, n, tmp);
+    launch_k(k_scan_top, dim3(1), dim3(1024), 0, tmp, nb);
+    launch_k(k_scan_down, dim3((unsigned)nb), dim3(kBlock), 0, in, n, (const int32_t *)tmp, out, out2);
     rt_after_launch(K_SCAN);
 }
 
@@ -611,9 +634,10 @@ template <typename T> class Sys final : public StateI {
                 attr = true;
             }
             rt_before_launch(K_RANK);
-            k_rebuild_small<T><<<1, kRebuildSmallThreads, smem, rt_stream()>>>(
-                (int)N_, (int)ncell, hinst[0], check, pos[cur].p, vel[cur].p, pos[nxt].p,
-                vel[nxt].p, xref.p, perm.p, invperm.p, cellStart.p, ex0, ex0N, ex1, ex1N, flags.p);
+            launch_k(k_rebuild_small<T>, dim3(1), dim3(kRebuildSmallThreads), smem, (int)N_,
+                     (int)ncell, hinst[0], check, (const T2<T> *)pos[cur].p,
+                     (const T2<T> *)vel[cur].p, pos[nxt].p, vel[nxt].p, xref.p, perm.p,
+                     invperm.p, cellStart.p, ex0, ex0N, ex1, ex1N, flags.p);
             rt_after_launch(K_RANK);
             cur = nxt;
             build_masks();
@@ -736,8 +760,8 @@ template <typename T> class Sys final : public StateI {
         if (form == 1 && B == 1) {
             const int bs = 32 * kTileWarps;
             rt_before_launch(K_DENSITY);
-            k_density_tile<T><<<(unsigned)((N_ + bs - 1) / bs), bs, 0, rt_stream()>>>(
-                v, rhoOut, prhoOut, tmask.p);
+            launch_k(k_density_tile<T>, dim3((unsigned)((N_ + bs - 1) / bs)), dim3(bs), 0, v,
+                     rhoOut, prhoOut, tmask.p);
             rt_after_launch(K_DENSITY);
             return;
         }
@@ -906,6 +930,7 @@ template <typename T>
 __global__ void k_list_neighbors(NLView<T> v, const int32_t *__restrict__ perm,
                                  int32_t *__restrict__ out, int32_t *__restrict__ nbc)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     const int32_t id = perm[i];
@@ -939,6 +964,7 @@ __global__ void k_objective(int64_t n, int64_t off, int kind, const int32_t *__r
                             T Lx, T a0, T a1, T a2, T2<T> *__restrict__ seedX,
                             T2<T> *__restrict__ seedV, double *__restrict__ partial)
 {
+    pdl_enter();
     const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t t = off + k;
     double j = 0.0;
@@ -976,6 +1002,7 @@ __global__ void k_objective(int64_t n, int64_t off, int kind, const int32_t *__r
 static __global__ void k_sum_partials(int64_t nb, const double *__restrict__ partial,
                                       double *__restrict__ out)
 {
+    pdl_enter();
     __shared__ double sm[kBlock];
     double a = 0.0;
     for (int64_t i = threadIdx.x; i < nb; i += blockDim.x) a += partial[i];
@@ -1178,9 +1205,10 @@ template <typename T> class Work final : public WorkI {
             const unsigned gN = grid_for(N_);
             const unsigned gT = grid_for(nnode);
             rt_before_launch(K_GATHER);
-            k_gather_theta<T><<<gN + gT, kBlock, 0, rt_stream()>>>(
-                N_, gN, S.perm.p, srcInv, sx, sv, S.pos[S.cur].p, S.vel[S.cur].p, nnode, S.B,
-                S.dinst.p, thetaAcc.p, emax.p, pendingTheta, gtheta.p);
+            launch_k(k_gather_theta<T>, dim3(gN + gT), dim3(kBlock), 0, N_, gN,
+                     (const int32_t *)S.perm.p, srcInv, sx, sv, S.pos[S.cur].p, S.vel[S.cur].p,
+                     nnode, S.B, (const Inst<T> *)S.dinst.p, thetaAcc.p, emax.p, pendingTheta,
+                     gtheta.p);
             rt_after_launch(K_GATHER);
             pendingTheta = -1;
         } else {
@@ -1278,7 +1306,8 @@ template <typename T> class Work final : public WorkI {
                        a2, devSeedX.p, devSeedV.p, partial.p + pofs);
             const int64_t nb = grid_for(I.n);
             rt_before_launch(K_MISC);
-            k_sum_partials<<<1, kBlock, 0, rt_stream()>>>(nb, partial.p + pofs, partial.p + nbTot + b);
+            launch_k(k_sum_partials, dim3(1), dim3(kBlock), 0, nb, (const double *)(partial.p + pofs),
+                     partial.p + nbTot + b);
             rt_after_launch(K_MISC);
             pofs += nb;
         }

@@ -93,6 +93,9 @@ void rt_set_group_lanes(int lanes);
 // arithmetic.
 int rt_density_form();
 void rt_set_density_form(int form);
+// Programmatic dependent launch of the engine's kernels (default on).
+bool rt_launch_overlap();
+void rt_set_launch_overlap(bool on);
 // True while the calling thread records its library stream into a CUDA graph:
 // host reads and synchronisations are skipped (results stay on the device)
 // and device allocations are refused.

@@ -105,6 +105,7 @@ __device__ __forceinline__ int32_t block_excl_scan(int32_t v, int32_t *smem_warp
 
 static __global__ void k_scan_reduce(const int32_t *__restrict__ in, int64_t n, int32_t *__restrict__ bsum)
 {
+    pdl_enter();
     __shared__ int32_t sw[33];
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     int32_t s = 0;
@@ -121,6 +122,7 @@ static __global__ void k_scan_reduce(const int32_t *__restrict__ in, int64_t n, 
 // single block: exclusive scan of nb block sums in place
 static __global__ void k_scan_top(int32_t *__restrict__ bsum, int64_t nb)
 {
+    pdl_enter();
     __shared__ int32_t sw[33];
     int32_t carry = 0;
     for (int64_t base = 0; base < nb; base += blockDim.x) {
@@ -138,6 +140,7 @@ static __global__ void k_scan_down(const int32_t *__restrict__ in, int64_t n,
                             const int32_t *__restrict__ bsum, int32_t *__restrict__ out,
                             int32_t *__restrict__ out2)
 {
+    pdl_enter();
     __shared__ int32_t sw[33];
     constexpr int IPT = kScanTile / kBlock;
     const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * IPT;
@@ -179,6 +182,7 @@ __global__ void k_assign(int64_t N, const T2<T> *__restrict__ pos, const T2<T> *
                          const uint16_t *__restrict__ pinst, int32_t *__restrict__ cellTmp,
                          int32_t *__restrict__ counts, uint32_t *__restrict__ flags)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < N;
     int32_t c = -1;
@@ -210,6 +214,7 @@ static __global__ void k_bucket(int64_t N, const int32_t *__restrict__ cellTmp,
                                 const int32_t *__restrict__ perm, int32_t *__restrict__ cursor,
                                 int32_t *__restrict__ bucketSrc, int32_t *__restrict__ bucketId)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < N;
     const int32_t c = live ? cellTmp[i] : -1;
@@ -239,6 +244,7 @@ __global__ void k_rank_permute(int64_t N, const int32_t *__restrict__ cellTmp,
                                T2<T> *__restrict__ ex0N, const T2<T> *__restrict__ ex1,
                                T2<T> *__restrict__ ex1N)
 {
+    pdl_enter();
     const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= N) return;
     const int32_t src = bucketSrc[s];
@@ -280,6 +286,7 @@ __global__ void __launch_bounds__(kRebuildSmallThreads)
                     const T2<T> *__restrict__ ex1, T2<T> *__restrict__ ex1N,
                     uint32_t *__restrict__ flags)
 {
+    pdl_enter();
     extern __shared__ int32_t sm[];
     int32_t *cursor = sm;                  // ncell: counts, then running cursors
     int32_t *starts = cursor + ncell;      // ncell + 1
@@ -394,6 +401,7 @@ __global__ void k_nl_build(int64_t N, const Inst<T> one, const Inst<T> *__restri
                            uint32_t *__restrict__ masks, int32_t *__restrict__ nbcount,
                            uint32_t *__restrict__ flags)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const int bi = MULTI ? (int)pinst[i] : 0;
@@ -708,6 +716,7 @@ __global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 6 : 4)
     k_density_eos(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
                   T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     density_walk<T, MULTI, PAIRS>(v, i, rho, prho, tmaskOut);
@@ -859,6 +868,7 @@ __global__ void __launch_bounds__(32 * kTileWarps)
     k_density_tile(const __grid_constant__ NLView<T> v, T *__restrict__ rho,
                    T2<T> *__restrict__ prho, uint32_t *__restrict__ tmaskOut)
 {
+    pdl_enter();
     __shared__ T2<T> stage[kTileWarps][kTileStage];
     const int w = (int)(threadIdx.x >> 5);
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1012,6 +1022,7 @@ __global__ void __launch_bounds__(kBlock)
                       const int32_t *__restrict__ perm, T2<T> *__restrict__ tx,
                       T2<T> *__restrict__ tv)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     const int b = MULTI ? inst_of(v, i) : 0;
@@ -1066,6 +1077,7 @@ __global__ void k_gather_state(int64_t N, const int32_t *__restrict__ perm,
                                const T2<T> *__restrict__ sx, const T2<T> *__restrict__ sv,
                                T2<T> *__restrict__ pos, T2<T> *__restrict__ vel)
 {
+    pdl_enter();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     int32_t s = perm[t];
@@ -1079,6 +1091,7 @@ template <typename T>
 __global__ void k_scatter_to_ids(int64_t N, const int32_t *__restrict__ perm,
                                  const T2<T> *__restrict__ a, T2<T> *__restrict__ out)
 {
+    pdl_enter();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     out[perm[t]] = a[t];
@@ -1088,6 +1101,7 @@ template <typename T>
 __global__ void k_scatter_to_ids1(int64_t N, const int32_t *__restrict__ perm,
                                   const T *__restrict__ a, T *__restrict__ out)
 {
+    pdl_enter();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     out[perm[t]] = a[t];
@@ -1097,6 +1111,7 @@ template <typename T>
 __global__ void k_gather_from_ids(int64_t N, const int32_t *__restrict__ perm,
                                   const T2<T> *__restrict__ a, T2<T> *__restrict__ out)
 {
+    pdl_enter();
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= N) return;
     out[t] = a[perm[t]];
@@ -1147,6 +1162,7 @@ __global__ void __launch_bounds__(kBlock)
                      T2<T> *__restrict__ gV, T2<T> *__restrict__ abar, T *__restrict__ galpha,
                      int *__restrict__ emax, int parity)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool live = i < v.N;
     int e = INT_MIN;
@@ -1200,6 +1216,7 @@ __global__ void __launch_bounds__(kBlock, (sizeof(T) == 4 && !MULTI && !AV) ? 5 
                    const T *__restrict__ galpha, T2<T> *__restrict__ gXs, T *__restrict__ grho,
                    T2<T> *__restrict__ gV)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     decltype(auto) I = load_inst<MULTI>(v, i);
@@ -1368,6 +1385,7 @@ __global__ void __launch_bounds__(kBlock)
                  const int *__restrict__ emax, int parity,
                  unsigned long long *__restrict__ thetaAcc)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= v.N) return;
     const int b = MULTI ? inst_of(v, i) : 0;
@@ -1489,6 +1507,7 @@ __global__ void k_theta_node(int64_t nnode, int B, const Inst<T> *__restrict__ i
                              unsigned long long *__restrict__ acc, int *__restrict__ emax,
                              int parity, double *__restrict__ gtheta)
 {
+    pdl_enter();
     theta_node<T>((int64_t)blockIdx.x * blockDim.x + threadIdx.x, nnode, B, inst, acc, emax,
                   parity, gtheta);
 }
@@ -1504,6 +1523,7 @@ __global__ void k_gather_theta(int64_t N, unsigned gridN, const int32_t *__restr
                                unsigned long long *__restrict__ acc, int *__restrict__ emax,
                                int parity, double *__restrict__ gtheta)
 {
+    pdl_enter();
     if (blockIdx.x < gridN) {
         const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
         if (t >= N) return;
@@ -1519,6 +1539,7 @@ __global__ void k_gather_theta(int64_t N, unsigned gridN, const int32_t *__restr
 
 static __global__ void k_fill_int(int64_t n, int *__restrict__ a, int v)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) a[i] = v;
 }
@@ -1526,6 +1547,7 @@ static __global__ void k_fill_int(int64_t n, int *__restrict__ a, int v)
 template <typename T>
 __global__ void k_to_T(int64_t n, const double *__restrict__ a, T *__restrict__ out)
 {
+    pdl_enter();
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = (T)a[i];
 }

@@ -61,3 +61,26 @@ def test_density_forms_match_the_mask_walk(one_thread, name, form):
             assert np.array_equal(out[form][k], out["mask"][k]), k
         else:
             assert K.relerr(out[form][k], out["mask"][k]) <= 1e-5, k
+
+
+@pytest.mark.parametrize("dtype,lanes", [("f64", 0), ("f32", 0), ("f32", 1)])
+def test_launch_overlap_does_not_change_results(dtype, lanes):
+    """Programmatic dependent launch only moves when a kernel is scheduled;
+    every kernel waits for its predecessor's results, so the results are the
+    same bits with and without it (small states: lane-group kernels, or one
+    thread per particle; the cell list is rebuilt every other step)."""
+    case = K.dambreak_case(theta_seed=4, jitter=0.05)
+    rng = np.random.default_rng(5)
+    case["cX"] = rng.standard_normal(case["X0"].shape)
+    case["cV"] = rng.standard_normal(case["X0"].shape)
+    S.set_group_lanes(lanes)
+    out = {}
+    try:
+        for on in (False, True):
+            S.set_launch_overlap(on)
+            out[on] = run_gpu(case, 30, dtype=dtype, seeds=linear_seeds(case), interval=2)
+    finally:
+        S.set_launch_overlap(True)
+        S.set_group_lanes(0)
+    for k in ("X", "V", "gX", "gV", "gtheta"):
+        assert np.array_equal(out[True][k], out[False][k]), k
