@@ -9,10 +9,10 @@
 // lock step, one step of each per tick, and runs each pass of the tick as ONE
 // grouped launch over the particles of every request that takes part: one
 // launch for all the gathers, one for each cell-list stage of the requests
-// whose neighbour list is due, one density pass, one force pass (the forward
-// accel + integrate of requests in their forward phase and the accel + drag
-// VJP of requests in their reverse phase, chosen per block), one pass 1, one
-// pass 2 and one design-node flush. Requests join at the next tick after
+// whose neighbour list is due, one density pass, the force passes (one for the
+// forward accel + integrate of requests in their forward phase, one for the
+// accel + drag VJP of requests in their reverse phase), one pass 1, one pass 2
+// and one design-node flush. Requests join at the next tick after
 // admission and leave when their program ends, so the set sharing a launch
 // changes continuously.
 //
@@ -82,9 +82,9 @@ template <typename T> struct GSys {
 #error "define SPH_PACK_T (this translation unit's precision) before including sph_pack.cuh"
 #endif
 constexpr int kMaxPackSys = 64; // requests one tick can hold
-constexpr int kPackLists = 8;
+constexpr int kPackLists = 9;
 enum PackList : int {
-    PL_GATHER = 0, PL_CELLS, PL_SCANTOP, PL_SCANTILE, PL_PART, PL_ALL, PL_REV, PL_THETA
+    PL_GATHER = 0, PL_CELLS, PL_SCANTOP, PL_SCANTILE, PL_PART, PL_ALL, PL_REV, PL_THETA, PL_FWD
 };
 struct PackLists {
     int32_t cnt[kPackLists];
@@ -305,28 +305,37 @@ __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 10 : 1)
     density_walk<T, false, true>(v, i, d.rho, d.prho, d.tmask);
 }
 
-// accel_kernel! + integrate_kernel! (forward requests) or the accel
-// recompute + _adj_integrate! + _adj_drag! (reverse requests), per block
+// accel_kernel! + integrate_kernel! of the requests taking a forward step.
+// The forward and reverse force passes are separate kernels so that each gets
+// the registers of its own body (one kernel holding both spilled).
 template <typename T, bool AV>
 __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
-    g_accel(int l)
+    g_accel_fwd(int l)
+{
+    const int2 f = glist_find(l);
+    const GSys<T> &d = pack_sys<T>(f.x);
+    const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
+    if (i >= d.n) return;
+    const NLView<T> &v = d.v;
+    const Inst<T> &I = v.one;
+    const T2<T> xi = v.pos[i];
+    const T2<T> vi = d.vel[i];
+    T ax, ay;
+    accel_sum<T, AV>(v, I, d.vel, d.prho, d.rhoAll, i, xi, vi, ax, ay);
+    accel_integrate_finish<T>(I, 0, i, xi, vi, ax, ay, d.theta, d.posOut, d.velOut,
+                              (T2<T> *)nullptr, (T *)nullptr, d.flags, d.perm, d.tx, d.tv);
+}
+
+// accel recompute + _adj_integrate! + _adj_drag! of the requests taking a
+// reverse step, with the largest exponent of |galpha| (one atomic per warp)
+template <typename T, bool AV>
+__global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 12 : 1)
+    g_accel_rev(int l)
 {
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
     const bool live = i < d.n;
-    if (d.mode == 0) {
-        if (!live) return;
-        const NLView<T> &v = d.v;
-        const Inst<T> &I = v.one;
-        const T2<T> xi = v.pos[i];
-        const T2<T> vi = d.vel[i];
-        T ax, ay;
-        accel_sum<T, AV>(v, I, d.vel, d.prho, d.rhoAll, i, xi, vi, ax, ay);
-        accel_integrate_finish<T>(I, 0, i, xi, vi, ax, ay, d.theta, d.posOut, d.velOut,
-                                  (T2<T> *)nullptr, (T *)nullptr, d.flags, d.perm, d.tx, d.tv);
-        return;
-    }
     int e = INT_MIN;
     if (live) {
         const NLView<T> &v = d.v;
@@ -337,7 +346,6 @@ __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
         accel_sum<T, AV>(v, I, d.vel, d.prho, d.rhoAll, i, xi, vi, ax, ay);
         e = drag_adj_finish<T>(I, i, xi, vi, ax, ay, d.theta, d.gX, d.gV, d.abar, d.galpha);
     }
-    // largest exponent of |galpha| over the warp, one atomic per warp
     const unsigned act = __ballot_sync(0xffffffffu, live);
     if (!live) return;
     int mx = e;
@@ -652,7 +660,7 @@ template <typename T> class Packer final : public PackI {
             }
             int32_t blocks() const { return start.back(); }
         };
-        List lGather, lCells, lScanTop, lScanTile, lPart, lAll, lRev, lTheta;
+        List lGather, lCells, lScanTop, lScanTile, lPart, lAll, lRev, lTheta, lFwd;
         bool anyAV = false;
         auto nb = [](int64_t n, int b) { return (n + b - 1) / b; };
         for (int k = 0; k < P; ++k) {
@@ -750,6 +758,7 @@ template <typename T> class Packer final : public PackI {
                 lPart.add(k, nb(N, kPackBlock));
             }
             lAll.add(k, nb(N, kPackBlock));
+            if (!rev) lFwd.add(k, nb(N, kPackBlock));
             // host bookkeeping of maybe_rebuild! and the step
             if (rebuild) Y.age = 0;
             Y.age += 1;
@@ -761,8 +770,8 @@ template <typename T> class Packer final : public PackI {
         Ring &R = ring_[ringPos_];
         ringPos_ = (ringPos_ + 1) % kRing;
         if (R.used) SPH_CK(cudaEventSynchronize(R.ev));
-        const List *lists[kPackLists] = {&lGather, &lCells, &lScanTop, &lScanTile,
-                                         &lPart, &lAll, &lRev, &lTheta};
+        const List *lists[kPackLists] = {&lGather, &lCells, &lScanTop, &lScanTile, &lPart,
+                                         &lAll, &lRev, &lTheta, &lFwd};
         const size_t bytes = sizeof(PackLists) + sizeof(GSys<T>) * (size_t)P;
         if (!R.host) {
             SPH_CK(cudaHostAlloc((void **)&R.host, sizeof(PackTable<T>), cudaHostAllocDefault));
@@ -796,8 +805,10 @@ template <typename T> class Packer final : public PackI {
         launch(K_RANK, PL_PART, kPackBlock, g_rank<T>);
         launch(K_NLBUILD, PL_PART, kPackBlock, g_nl_build<T>);
         launch(K_DENSITY, PL_ALL, kPackBlock, g_density<T>);
-        if (anyAV) launch(K_ACCEL_DRAG, PL_ALL, kPackBlock, g_accel<T, true>);
-        else launch(K_ACCEL_DRAG, PL_ALL, kPackBlock, g_accel<T, false>);
+        if (anyAV) launch(K_ACCEL_INTEGRATE, PL_FWD, kPackBlock, g_accel_fwd<T, true>);
+        else launch(K_ACCEL_INTEGRATE, PL_FWD, kPackBlock, g_accel_fwd<T, false>);
+        if (anyAV) launch(K_ACCEL_DRAG, PL_REV, kPackBlock, g_accel_rev<T, true>);
+        else launch(K_ACCEL_DRAG, PL_REV, kPackBlock, g_accel_rev<T, false>);
         if (anyAV) launch(K_PASS1, PL_REV, kPackBlock, g_pass1<T, true>);
         else launch(K_PASS1, PL_REV, kPackBlock, g_pass1<T, false>);
         launch(K_PASS2, PL_REV, kPackBlock, g_pass2<T>);
