@@ -430,7 +430,16 @@ __device__ __forceinline__ void nl_build_one(int64_t N, const IT &I, int bi, int
     uint32_t spill = 0;
     auto pass = [&](int j) -> uint32_t {
         const T2<T> xj = pos[j];
-        const T r2 = r2_exact<T>(sub_rn(xi.x, xj.x), sub_rn(xi.y, xj.y));
+        T r2;
+        if constexpr (sizeof(T) == 4 && kPackedPairs) {
+            // the same separately rounded difference, squares and sum, with
+            // the x and y halves in one f32x2 instruction each
+            const float2 d = fsub2(xi, xj);
+            const float2 q = fmul2(d, d);
+            r2 = add_rn(q.x, q.y);
+        } else {
+            r2 = r2_exact<T>(sub_rn(xi.x, xj.x), sub_rn(xi.y, xj.y));
+        }
         return (r2min < r2 && r2 < rc2) ? 1u : 0u;
     };
     uint32_t lo[3], hi[3];
