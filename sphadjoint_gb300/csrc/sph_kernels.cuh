@@ -1218,7 +1218,7 @@ __device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T>
 // adj_design_kernel! (gXs += galpha * grad alpha, src/adjoint.jl:173-175)
 // + _axpy2!(gV, gVs).
 template <typename T, bool MULTI, bool AV = false>
-__global__ void __launch_bounds__(kBlock, (sizeof(T) == 4 && !MULTI && !AV) ? 5 : 1) // single FP32: <= 51 registers (4% faster)
+__global__ void __launch_bounds__(kBlock, (sizeof(T) == 4 && !MULTI && !AV) ? 6 : 1) // single FP32: <= 42 registers
     k_pass1_design(const __grid_constant__ NLView<T> v, const T2<T> *__restrict__ vel,
                    const T2<T> *__restrict__ prho, const T *__restrict__ rho,
                    const T *__restrict__ theta, const T2<T> *__restrict__ abar,
