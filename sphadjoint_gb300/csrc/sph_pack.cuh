@@ -37,6 +37,7 @@
 namespace sphgb {
 
 constexpr int kPackBlock = 128; // threads per block of the per-particle grouped kernels
+constexpr bool kAlignRebuilds = true; // start sweeps on ticks aligned to the rebuild interval
 
 // One request's arrays and constants for one tick.
 template <typename T> struct GSys {
@@ -514,6 +515,7 @@ template <typename T> class Packer final : public PackI {
         std::unique_ptr<Tape<T>> tape;
         std::vector<PackOp> prog;
         size_t pc = 0;
+        bool fwdStarted = false, revStarted = false;
         int gcur = 0;
         int64_t rstep = 0;
         bool finishing = false;
@@ -639,9 +641,25 @@ template <typename T> class Packer final : public PackI {
             Req &q = *kv.second;
             if (q.finishing) continue;
             const PackOp op = advance(q);
-            if (op.kind == OP_FINISH) finish(q);
-            else parts.push_back({&q, op});
+            if (op.kind == OP_FINISH) {
+                finish(q);
+                continue;
+            }
+            // Start each sweep on a tick that is a multiple of the request's
+            // rebuild interval: its state is rebuilt on its first step and
+            // every interval steps after, so requests started this way
+            // rebuild on the same ticks and share one set of cell-list
+            // launches (otherwise every phase of the interval pays its own
+            // small launches). Waiting moves only when the step runs.
+            bool &started = op.kind == OP_FWD ? q.fwdStarted : q.revStarted;
+            if (kAlignRebuilds && !started && ticks_ % q.spec.opts.interval != 0) {
+                --q.pc;
+                continue;
+            }
+            started = true;
+            parts.push_back({&q, op});
         }
+        ++ticks_;
         if (parts.empty()) return 0;
         const int P = (int)parts.size();
         if (P > kMaxPackSys)
@@ -816,7 +834,6 @@ template <typename T> class Packer final : public PackI {
         SPH_CK(cudaEventRecord(R.ev, st));
         R.used = true;
         rt_check_launch("packed tick");
-        ++ticks_;
         return P;
     }
 
