@@ -1366,6 +1366,42 @@ __device__ __forceinline__ void fixed_add(unsigned long long *acc, double c, int
     if (h) atomicAdd(acc + 1, h);
 }
 
+// fixed_add of an FP32 contribution with integer instructions only: c is
+// M 2^E with a 24-bit integer M, so round(|c| 2^S) is M shifted by E + S,
+// rounded half to even when the shift drops bits, which is what the double
+// path's rint(ldexp(|c|, S)) gives for a float c (the double product is
+// exact). The same 128-bit integer reaches the accumulator without the
+// double-precision pipe, which runs at a small fraction of the FP32 rate.
+__device__ __forceinline__ void fixed_add(unsigned long long *acc, float c, int S)
+{
+    const uint32_t bits = __float_as_uint(c);
+    const uint32_t ex = (bits >> 23) & 0xffu;
+    if ((bits & 0x7fffffffu) == 0u || ex == 0xffu) return; // zero, inf, NaN
+    const uint32_t M = ex ? ((bits & 0x7fffffu) | 0x800000u) : (bits & 0x7fffffu);
+    const int k = (ex ? (int)ex - 150 : -149) + S;
+    if (k >= 104) { // beyond the 128-bit grid (cannot happen by the scale's bound)
+        fixed_add(acc, (double)c, S);
+        return;
+    }
+    unsigned __int128 v;
+    if (k >= 0) {
+        v = (unsigned __int128)M << k;
+    } else if (k <= -25) {
+        return; // below half a unit of the grid: rounds to 0
+    } else {
+        const int sh = -k;
+        const uint32_t q = M >> sh, r = M & ((1u << sh) - 1u), half = 1u << (sh - 1);
+        const uint32_t up = (r > half || (r == half && (q & 1u))) ? 1u : 0u;
+        v = (unsigned __int128)(q + up);
+    }
+    if (v == 0) return;
+    if (bits >> 31) v = ~v + 1;
+    const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
+    const unsigned long long old = atomicAdd(acc, lo);
+    const unsigned long long h = hi + ((old + lo < old) ? 1ull : 0ull);
+    if (h) atomicAdd(acc + 1, h);
+}
+
 // Scale 2^S of the fixed-point grid: every contribution of the step is below
 // 2^emax and at most n of them reach one node, so sums stay below 2^124.
 __host__ __device__ __forceinline__ int theta_scale(int emax, int lgN) { return 124 - emax - lgN; }
@@ -1470,10 +1506,11 @@ __device__ __forceinline__ void pass2_finish(const IT &I, int b, int64_t i, cons
         const int S = theta_scale(em, I.lgN);
         unsigned long long *acc = thetaAcc + 2 * (int64_t)I.toff;
         const int64_t l00 = (int64_t)j0 + (int64_t)i0 * p.ngy;
-        fixed_add(acc + 2 * l00, (double)(ga * ((T)1 - fx) * ((T)1 - fy)), S);
-        fixed_add(acc + 2 * (l00 + p.ngy), (double)(ga * fx * ((T)1 - fy)), S);
-        fixed_add(acc + 2 * (l00 + 1), (double)(ga * ((T)1 - fx) * fy), S);
-        fixed_add(acc + 2 * (l00 + p.ngy + 1), (double)(ga * fx * fy), S);
+        // T-typed contributions: FP32 ones take the integer conversion
+        fixed_add(acc + 2 * l00, ga * ((T)1 - fx) * ((T)1 - fy), S);
+        fixed_add(acc + 2 * (l00 + p.ngy), ga * fx * ((T)1 - fy), S);
+        fixed_add(acc + 2 * (l00 + 1), ga * ((T)1 - fx) * fy, S);
+        fixed_add(acc + 2 * (l00 + p.ngy + 1), ga * fx * fy, S);
     }
 }
 
