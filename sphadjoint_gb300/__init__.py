@@ -29,6 +29,9 @@ from .api import (  # noqa: F401
     set_group_lanes,
     set_density_form,
     set_launch_overlap,
+    set_step_graphs,
+    step_graphs,
+    step_graph_counts,
     density_form,
     simulate,
     step,

@@ -105,6 +105,9 @@ _SIGS = {
     "sph_set_group_lanes": (_I32, [_I32]),
     "sph_set_density_form": (_I32, [_I32]),
     "sph_set_launch_overlap": (_I32, [_I32]),
+    "sph_set_step_graphs": (_I32, [_I32]),
+    "sph_get_step_graphs": (_I32, [_I32P]),
+    "sph_step_graph_counts": (_I32, [_I64P, _I64P]),
     "sph_get_density_form": (_I32, [_I32P]),
     "sph_capture_begin": (_I32, []),
     "sph_capture_end": (_I32, [_PP]),

@@ -829,6 +829,28 @@ def set_launch_overlap(on: bool) -> None:
     L.check(L.load().sph_set_launch_overlap(1 if on else 0))
 
 
+def set_step_graphs(steps: int) -> None:
+    """Steps per recorded group (no counterpart in the reference),
+    process-wide: simulate and backward record the launches of this many
+    consecutive steps and replay each group as one CUDA graph (default 32;
+    0 launches every kernel on its own). Results do not depend on it."""
+    L.check(L.load().sph_set_step_graphs(int(steps)))
+
+
+def step_graphs() -> int:
+    v = C.c_int32()
+    L.check(L.load().sph_get_step_graphs(C.byref(v)))
+    return v.value
+
+
+def step_graph_counts() -> tuple:
+    """(groups replayed as graphs, graphs instantiated) since the library was
+    loaded, process-wide."""
+    r, i = C.c_int64(), C.c_int64()
+    L.check(L.load().sph_step_graph_counts(C.byref(r), C.byref(i)))
+    return r.value, i.value
+
+
 def density_form() -> str:
     v = C.c_int32()
     L.check(L.load().sph_get_density_form(C.byref(v)))

@@ -26,7 +26,10 @@ std::atomic<long long> g_launches{0};
 std::atomic<int> g_group_lanes{0};
 std::atomic<int> g_density_form{2};
 std::atomic<bool> g_launch_overlap{true};
+std::atomic<int> g_step_graph{32};
+std::atomic<long long> g_sg_replays{0}, g_sg_inst{0};
 thread_local bool g_capturing = false;
+thread_local bool g_recording = false;
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {};
 
@@ -118,11 +121,137 @@ void rt_after_launch(int kid)
 
 void rt_check_launch(const char *name) { cuda_check(cudaGetLastError(), name); }
 
-bool rt_capturing() { return g_capturing; }
+bool rt_capturing() { return g_capturing || g_recording; }
+bool rt_recording_steps() { return g_recording; }
+
+bool rt_timers_on()
+{
+    for (const KTimer &t : g_timer)
+        if (t.on) return true;
+    return false;
+}
 
 void rt_sync()
 {
-    if (!g_capturing) cuda_check(cudaStreamSynchronize(rt_stream()), "cudaStreamSynchronize");
+    if (!rt_capturing()) cuda_check(cudaStreamSynchronize(rt_stream()), "cudaStreamSynchronize");
+}
+
+int rt_step_graph() { return g_step_graph.load(std::memory_order_relaxed); }
+void rt_set_step_graph(int steps) { g_step_graph.store(steps, std::memory_order_relaxed); }
+
+// ---- groups of steps replayed as graphs ---------------------------------------
+StepGraphs::~StepGraphs()
+{
+    abandon();
+    for (Entry &e : cache_) (void)cudaGraphExecDestroy(e.exec);
+    (void)cudaGetLastError();
+}
+
+void StepGraphs::start(bool eligible)
+{
+    per_ = rt_step_graph();
+    on_ = eligible && per_ > 0 && !rt_capturing() && !rt_timers_on();
+    count_ = 0;
+}
+
+void StepGraphs::before_step()
+{
+    if (!on_ || open_) return;
+    cuda_check(cudaStreamBeginCapture(rt_stream(), cudaStreamCaptureModeThreadLocal),
+               "cudaStreamBeginCapture");
+    open_ = true;
+    g_recording = true;
+    count_ = 0;
+}
+
+void StepGraphs::after_step()
+{
+    if (!open_) return;
+    if (++count_ >= per_) replay();
+}
+
+void StepGraphs::finish()
+{
+    if (open_) replay();
+    on_ = false;
+}
+
+void StepGraphs::abandon() noexcept
+{
+    if (!open_) return;
+    open_ = false;
+    g_recording = false;
+    cudaGraph_t g = nullptr;
+    (void)cudaStreamEndCapture(rt_stream(), &g);
+    if (g) (void)cudaGraphDestroy(g);
+    (void)cudaGetLastError();
+}
+
+void StepGraphs::replay()
+{
+    open_ = false;
+    g_recording = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(rt_stream(), &g);
+    if (ec != cudaSuccess || !g) {
+        if (g) (void)cudaGraphDestroy(g);
+        cuda_check(ec != cudaSuccess ? ec : cudaErrorStreamCaptureInvalidated,
+                   "cudaStreamEndCapture (group of steps)");
+    }
+    struct Drop {
+        cudaGraph_t g;
+        ~Drop() { (void)cudaGraphDestroy(g); }
+    } drop{g};
+    // shape key: node count, node types and kernel functions in recording order
+    size_t n = 0;
+    cuda_check(cudaGraphGetNodes(g, nullptr, &n), "cudaGraphGetNodes");
+    if (n == 0) return;
+    std::vector<cudaGraphNode_t> nodes(n);
+    cuda_check(cudaGraphGetNodes(g, nodes.data(), &n), "cudaGraphGetNodes");
+    uint64_t key = 1469598103934665603ull ^ (uint64_t)n;
+    auto mix = [&](uint64_t v) { key = (key ^ v) * 1099511628211ull; };
+    for (cudaGraphNode_t nd : nodes) {
+        cudaGraphNodeType t;
+        cuda_check(cudaGraphNodeGetType(nd, &t), "cudaGraphNodeGetType");
+        mix((uint64_t)t);
+        if (t == cudaGraphNodeTypeKernel) {
+            cudaKernelNodeParams kp{};
+            cuda_check(cudaGraphKernelNodeGetParams(nd, &kp), "cudaGraphKernelNodeGetParams");
+            mix((uint64_t)(uintptr_t)kp.func);
+        }
+    }
+    Entry *hit = nullptr;
+    for (Entry &e : cache_)
+        if (e.key == key) hit = &e;
+    if (hit) {
+        cudaGraphExecUpdateResultInfo info{};
+        if (cudaGraphExecUpdate(hit->exec, g, &info) != cudaSuccess) {
+            (void)cudaGetLastError();
+            (void)cudaGraphExecDestroy(hit->exec);
+            hit->exec = nullptr;
+            cuda_check(cudaGraphInstantiate(&hit->exec, g, 0), "cudaGraphInstantiate");
+            inst_ += 1;
+            g_sg_inst.fetch_add(1, std::memory_order_relaxed);
+        }
+    } else {
+        constexpr size_t kMaxCached = 16;
+        if (cache_.size() >= kMaxCached) {
+            auto lru = std::min_element(cache_.begin(), cache_.end(),
+                                        [](const Entry &a, const Entry &b) { return a.used < b.used; });
+            (void)cudaGraphExecDestroy(lru->exec);
+            cache_.erase(lru);
+        }
+        cudaGraphExec_t x = nullptr;
+        cuda_check(cudaGraphInstantiate(&x, g, 0), "cudaGraphInstantiate");
+        inst_ += 1;
+        g_sg_inst.fetch_add(1, std::memory_order_relaxed);
+        cache_.push_back({key, x, 0});
+        hit = &cache_.back();
+    }
+    hit->used = ++clock_;
+    cuda_check(cudaGraphLaunch(hit->exec, rt_stream()), "cudaGraphLaunch");
+    replays_ += 1;
+    g_sg_replays.fetch_add(1, std::memory_order_relaxed);
 }
 
 int rt_group_lanes() { return g_group_lanes.load(std::memory_order_relaxed); }
@@ -642,6 +771,30 @@ SPH_API int32_t sph_set_launch_overlap(int32_t on)
     return guarded([&] {
         if (on != 0 && on != 1) throw Error(ERR_ARG, "launch overlap: 0 or 1");
         rt_set_launch_overlap(on == 1);
+    });
+}
+
+SPH_API int32_t sph_set_step_graphs(int32_t steps)
+{
+    return guarded([&] {
+        if (steps < 0) throw Error(ERR_ARG, "steps per recorded group must be >= 0");
+        rt_set_step_graph(steps);
+    });
+}
+
+SPH_API int32_t sph_get_step_graphs(int32_t *steps)
+{
+    return guarded([&] {
+        need(steps, "steps");
+        *steps = rt_step_graph();
+    });
+}
+
+SPH_API int32_t sph_step_graph_counts(int64_t *replays, int64_t *instantiations)
+{
+    return guarded([&] {
+        if (replays) *replays = (int64_t)g_sg_replays.load();
+        if (instantiations) *instantiations = (int64_t)g_sg_inst.load();
     });
 }
 

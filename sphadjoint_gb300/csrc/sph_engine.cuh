@@ -95,6 +95,18 @@ template <typename T> struct DevBuf {
 
 inline unsigned grid_for(int64_t n) { return (unsigned)((n + kBlock - 1) / kBlock); }
 
+// States whose simulate/backward steps go out as recorded groups (graphs):
+// every FP64 state and FP32 states of up to 2^18 particles. Measured per
+// fwd+adjoint solve, FP32: graphs 58.4 M particle-steps/s against 53.7 with
+// programmatic dependent launch at 2k particles, 1360 vs 1061 at 131k, 1771
+// vs 1735 at 262k, but 1478 vs 1558 at 1M; FP64: 18.8 vs 13.5 at 2k, 67.9 vs
+// 48.5 at 65k.
+constexpr int64_t kStepGraphMaxN32 = int64_t(1) << 18;
+template <typename T> inline bool step_graph_eligible(int64_t n)
+{
+    return sizeof(T) == 8 || n <= kStepGraphMaxN32;
+}
+
 // Launch on the library stream. Outside graph capture, and unless switched off
 // (sph_set_launch_overlap), kernels go out with programmatic dependent launch:
 // each may be scheduled while its predecessor still runs and waits on the
@@ -322,6 +334,7 @@ template <typename T> class Sys final : public StateI {
     DevBuf<int32_t> clStart, clOrder; // build! without a neighbour rebuild
     bool cellsOnlyLatest = false;
     bool keepAccel = false;
+    StepGraphs graphs;   // simulate's steps, replayed in groups
     bool anyRho = false; // some instance's model reads densities in the adjoint
     bool anyAV = false;  // some instance uses the artificial viscosity
 
@@ -462,6 +475,18 @@ template <typename T> class Sys final : public StateI {
         masks.zero();
         center.zero();
         cellStart.zero();
+        if (sizeof(T) == 4) {
+            // the one-launch cell list of small FP32 states (set here, outside
+            // any graph recording)
+            static bool attr = false;
+            if (!attr) {
+                SPH_CK(cudaFuncSetAttribute(k_rebuild_small<T>,
+                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)(sizeof(int32_t) * (2 * kRebuildSmallMaxCells + 1 +
+                                                                     3 * kRebuildSmallMaxN))));
+                attr = true;
+            }
+        }
         init_identity();
         if (X0 || V0) set(X0, V0);
         else {
@@ -625,14 +650,6 @@ template <typename T> class Sys final : public StateI {
             // coordinates cost more than the launches saved)
             const int nxt = 1 - cur;
             const size_t smem = sizeof(int32_t) * (size_t)(2 * ncell + 1 + 3 * N_);
-            static bool attr = false;
-            if (!attr) {
-                SPH_CK(cudaFuncSetAttribute(k_rebuild_small<T>,
-                                            cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            (int)(sizeof(int32_t) * (2 * kRebuildSmallMaxCells + 1 +
-                                                                     3 * kRebuildSmallMaxN))));
-                attr = true;
-            }
             rt_before_launch(K_RANK);
             launch_k(k_rebuild_small<T>, dim3(1), dim3(kRebuildSmallThreads), smem, (int)N_,
                      (int)ncell, hinst[0], check, (const T2<T> *)pos[cur].p,
@@ -855,9 +872,13 @@ template <typename T> class Sys final : public StateI {
     void sync() override { SPH_CK(cudaStreamSynchronize(rt_stream())); }
 
     // ---- snapshots ----
-    void save(Snap<T> &s)
+    void reserve(Snap<T> &s)
     {
         if (!s.blob.p) s.blob.alloc(core.n);
+    }
+    void save(Snap<T> &s)
+    {
+        reserve(s);
         s.blob.copy_from(core);
         s.age = age;
         s.cur = cur;
@@ -1099,7 +1120,15 @@ void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tap
                                           std::to_string(tp->n_ + nsteps) + " steps needed");
         tp->bind(*this);
     }
+    // the snapshot slots this call fills, allocated before any recording
+    if (tp && tp->nsnap_)
+        for (size_t k = 0; k < tp->descent.size(); ++k)
+            if (tp->descent[k] >= tp->n_ && tp->descent[k] < tp->n_ + nsteps)
+                reserve(tp->slot((int)k));
+    graphs.start(step_graph_eligible<T>(N_));
+    StepGraphsGuard guard{graphs};
     for (int64_t s = 0; s < nsteps; ++s) {
+        graphs.before_step();
         T2<T> *tx = nullptr, *tv = nullptr;
         if (tp) {
             const int64_t n = tp->n_;
@@ -1116,7 +1145,9 @@ void Sys<T>::simulate(FieldI *theta, const Params *p, int64_t nsteps, TapeI *tap
             tp->n_ += 1;
         }
         step_impl(th->th.p, tx, tv);
+        graphs.after_step();
     }
+    graphs.finish();
     rt_sync();
     rt_check_launch("simulate");
 }
@@ -1149,6 +1180,7 @@ template <typename T> class Work final : public WorkI {
     int64_t jOff = -1;       // J slots of the last objective in `partial`
     bool haveResult = false;
     bool haveDevSeeds = false;
+    StepGraphs graphs; // backward's steps, replayed in groups
 
     Work(int64_t N, const Params &p) : Work(std::vector<Params>{p}, std::vector<int64_t>{N}) {}
 
@@ -1544,11 +1576,18 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
     pendingTheta = -1;
     int64_t rstep = 0; // reverse steps done (parity of the exponent slot)
     tp->fwdSteps = 0;
+    // reverse steps and recomputed forward steps go out in recorded groups
+    if (tp->nsnap_ && L > 0)
+        for (int k = 0; k < tp->nsnap_; ++k) tp->recomp->reserve(tp->slot(k));
+    graphs.start(step_graph_eligible<T>(N_));
+    StepGraphsGuard guard{graphs};
     if (tp->nsnap_ == 0) {
         for (int64_t n = L - 1; n >= 0; --n) {
+            graphs.before_step();
             reverse_step(*S, th->th.p, tp->hx.p + (size_t)n * N_, tp->hv.p + (size_t)n * N_,
                          nullptr, (int)(rstep & 1));
             ++rstep;
+            graphs.after_step();
         }
     } else if (L > 0) {
         Sys<T> &R = *tp->recomp;
@@ -1567,7 +1606,11 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
             if (tp->slotPos[k] < 0 || tp->slotPos[k] >= L) freeSlots.push_back(k);
         int64_t rpos = -1; // step the recompute state holds (-1: unknown)
         auto advance = [&](int64_t m) {
-            for (int64_t s = 0; s < m; ++s) R.step_impl(th->th.p, nullptr, nullptr);
+            for (int64_t s = 0; s < m; ++s) {
+                graphs.before_step();
+                R.step_impl(th->th.p, nullptr, nullptr);
+                graphs.after_step();
+            }
             tp->fwdSteps += m;
             rpos += m;
         };
@@ -1581,9 +1624,11 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
         };
         auto rev_at_R = [&](int64_t n) {
             (void)n;
+            graphs.before_step();
             reverse_step(*S, th->th.p, R.pos[R.cur].p, R.vel[R.cur].p, R.invperm.p,
                          (int)(rstep & 1));
             ++rstep;
+            graphs.after_step();
         };
         // reverse steps [a, b) with the state at a in `slot`, c slots available
         // (including `slot`); recursion splits at plan_split.
@@ -1620,6 +1665,7 @@ void Work<T>::run_backward(TapeI *tape, FieldI *theta, const Params *pp, const v
             freeSlots.push_back(taken[k].second);
         }
     }
+    graphs.finish();
     flush_theta(*S);
     SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gX[gcur].p, outX.p);
     SPH_LAUNCH(K_MISC, k_scatter_to_ids<T>, N_, N_, S->perm.p, gV[gcur].p, outV.p);

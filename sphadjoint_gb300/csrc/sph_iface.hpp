@@ -96,10 +96,68 @@ void rt_set_density_form(int form);
 // Programmatic dependent launch of the engine's kernels (default on).
 bool rt_launch_overlap();
 void rt_set_launch_overlap(bool on);
-// True while the calling thread records its library stream into a CUDA graph:
-// host reads and synchronisations are skipped (results stay on the device)
-// and device allocations are refused.
+// Steps that simulate and backward record into one CUDA graph and replay
+// (0: every kernel is launched on its own; default 32).
+int rt_step_graph();
+void rt_set_step_graph(int steps);
+// True while the calling thread records its library stream into a CUDA graph
+// (a caller's capture or a group of steps): host reads and synchronisations
+// are skipped (results stay on the device) and device allocations are
+// refused.
 bool rt_capturing();
+// True while a group of steps is being recorded (not a caller's capture).
+bool rt_recording_steps();
+// True when any kernel timer is on (launches are then not grouped, so that
+// each one is timed on its own).
+bool rt_timers_on();
+
+// The launches of a sequence of steps (a solve's forward or reverse sweep),
+// recorded from the library stream in groups of rt_step_graph() steps; each
+// group is replayed as one CUDA graph as soon as it is complete, so the
+// device runs the same work in the same order as with direct launches, with
+// graph launch costs between the kernels. A group is recorded again on the
+// host every time (its pointers change) and replayed through an instantiated
+// graph of the same shape when one is cached (cudaGraphExecUpdate), else
+// through a new one.
+class StepGraphs {
+  public:
+    StepGraphs() = default;
+    StepGraphs(const StepGraphs &) = delete;
+    StepGraphs &operator=(const StepGraphs &) = delete;
+    ~StepGraphs();
+    // start of a sequence: grouping applies when `eligible`, the switch is
+    // on, the thread is not already capturing and no kernel timer is on
+    void start(bool eligible = true);
+    // around each step
+    void before_step();
+    void after_step();
+    // end of the sequence: replays the open group
+    void finish();
+    // error path: ends an open recording and drops it
+    void abandon() noexcept;
+    // groups replayed and graphs instantiated so far
+    int64_t replays() const { return replays_; }
+    int64_t instantiations() const { return inst_; }
+
+  private:
+    void replay();
+    struct Entry {
+        uint64_t key;
+        cudaGraphExec_t exec;
+        uint64_t used;
+    };
+    std::vector<Entry> cache_;
+    int per_ = 0, count_ = 0;
+    bool on_ = false, open_ = false;
+    uint64_t clock_ = 0;
+    int64_t replays_ = 0, inst_ = 0;
+};
+
+// Ends an open group of a StepGraphs when the scope is left by an exception.
+struct StepGraphsGuard {
+    StepGraphs &g;
+    ~StepGraphsGuard() { g.abandon(); }
+};
 // Wait for the library stream unless it is being captured.
 void rt_sync();
 

@@ -84,3 +84,42 @@ def test_launch_overlap_does_not_change_results(dtype, lanes):
         S.set_group_lanes(0)
     for k in ("X", "V", "gX", "gV", "gtheta"):
         assert np.array_equal(out[True][k], out[False][k]), k
+
+
+@pytest.mark.parametrize("dtype,lanes,snapshots", [("f64", 0, 0), ("f64", 0, 4), ("f32", 1, 3),
+                                                   ("f32", 0, 0)])
+def test_step_graphs_do_not_change_results(dtype, lanes, snapshots):
+    """simulate and backward replay their steps in recorded groups (CUDA
+    graphs); the groups hold the same launches in the same order as direct
+    launches, so results are the same bits and the launch count is the same,
+    for group sizes that do and do not divide the rebuild interval, with a
+    full tape and with checkpoints (restores, recomputed steps and snapshot
+    copies inside the groups)."""
+    case = K.dambreak_case(theta_seed=4, jitter=0.05)
+    rng = np.random.default_rng(6)
+    case["cX"] = rng.standard_normal(case["X0"].shape)
+    case["cV"] = rng.standard_normal(case["X0"].shape)
+    S.set_group_lanes(lanes)
+    out, launches = {}, {}
+    try:
+        for steps in (0, 1, 3, 32):
+            S.set_step_graphs(steps)
+            assert S.step_graphs() == steps
+            n0, (r0, _) = S.launch_count(), S.step_graph_counts()
+            out[steps] = run_gpu(case, 37, dtype=dtype, seeds=linear_seeds(case), interval=2,
+                                 snapshots=snapshots)
+            launches[steps] = S.launch_count() - n0
+            replays = S.step_graph_counts()[0] - r0
+            # forward steps and at least as many reverse steps, in groups
+            assert (replays == 0) == (steps == 0), (steps, replays)
+            if steps:
+                assert replays >= 2 * -(-37 // steps), (steps, replays)
+    finally:
+        S.set_step_graphs(32)
+        S.set_group_lanes(0)
+    for steps in (1, 3, 32):
+        assert launches[steps] == launches[0], steps
+        for k in ("X", "V", "gX", "gV", "gtheta"):
+            assert np.array_equal(out[steps][k], out[0][k]), (steps, k)
+    with pytest.raises(Exception):
+        S.set_step_graphs(-1)
