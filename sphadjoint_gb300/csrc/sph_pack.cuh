@@ -121,6 +121,7 @@ __device__ __forceinline__ int2 glist_find(int l)
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock) g_gather(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t t = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -133,6 +134,7 @@ __global__ void __launch_bounds__(kPackBlock) g_gather(int l)
 
 template <typename T> __global__ void __launch_bounds__(kBlock) g_zero_counts(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t c = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -143,6 +145,7 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_zero_counts(in
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock) g_assign(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -173,6 +176,7 @@ __global__ void __launch_bounds__(kPackBlock) g_assign(int l)
 // tile sums (one block each), then the tiles with their offsets
 template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_reduce(int l)
 {
+    pdl_enter();
     __shared__ int32_t sw[33];
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
@@ -190,6 +194,7 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_reduce(in
 
 template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_top(int l)
 {
+    pdl_enter();
     __shared__ int32_t sw[33];
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
@@ -207,6 +212,7 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_top(int l
 
 template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_down(int l)
 {
+    pdl_enter();
     __shared__ int32_t sw[33];
     constexpr int IPT = kScanTile / kBlock;
     const int2 f = glist_find(l);
@@ -238,6 +244,7 @@ template <typename T> __global__ void __launch_bounds__(kBlock) g_scan_down(int 
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock) g_bucket(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -258,6 +265,7 @@ __global__ void __launch_bounds__(kPackBlock) g_bucket(int l)
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock) g_rank(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t s = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -282,6 +290,7 @@ __global__ void __launch_bounds__(kPackBlock) g_rank(int l)
 template <typename T>
 __global__ void __launch_bounds__(kPackBlock) g_nl_build(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -297,6 +306,7 @@ template <typename T>
 __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 10 : 1)
     g_density(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -313,6 +323,7 @@ template <typename T, bool AV>
 __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 10 : 1)
     g_accel_fwd(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -333,6 +344,7 @@ template <typename T, bool AV>
 __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 12 : 1)
     g_accel_rev(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -361,6 +373,7 @@ template <typename T, bool AV>
 __global__ void __launch_bounds__(kPackBlock, (sizeof(T) == 4 && !AV) ? 9 : 1)
     g_pass1(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -383,6 +396,7 @@ template <typename T>
 __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 12 : 1)
     g_pass2(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     const int64_t i = (int64_t)f.y * blockDim.x + threadIdx.x;
@@ -398,6 +412,7 @@ __global__ void __launch_bounds__(kPackBlock, sizeof(T) == 4 ? 12 : 1)
 template <typename T>
 __global__ void __launch_bounds__(kBlock) g_theta(int l)
 {
+    pdl_enter();
     const int2 f = glist_find(l);
     const GSys<T> &d = pack_sys<T>(f.x);
     theta_node<T>((int64_t)f.y * blockDim.x + threadIdx.x, d.nnode, 1, &d.v.one, d.thetaAcc,
@@ -809,7 +824,7 @@ template <typename T> class Packer final : public PackI {
             const List &l = *lists[li];
             if (l.blocks() <= 0) return;
             rt_before_launch(kid);
-            kern<<<(unsigned)l.blocks(), bs, 0, st>>>(li);
+            launch_k(kern, dim3((unsigned)l.blocks()), dim3(bs), 0, li);
             rt_after_launch(kid);
             ++launches_;
         };
