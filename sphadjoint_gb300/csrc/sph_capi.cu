@@ -151,14 +151,28 @@ void StepGraphs::start(bool eligible)
 {
     per_ = rt_step_graph();
     on_ = eligible && per_ > 0 && !rt_capturing() && !rt_timers_on();
+    if (on_) {
+        // a stream the caller records with the CUDA API itself: its launches
+        // go into the caller's graph as they are
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(rt_stream(), &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+            (void)cudaGetLastError();
+            on_ = false;
+        }
+    }
     count_ = 0;
 }
 
 void StepGraphs::before_step()
 {
     if (!on_ || open_) return;
-    cuda_check(cudaStreamBeginCapture(rt_stream(), cudaStreamCaptureModeThreadLocal),
-               "cudaStreamBeginCapture");
+    // a stream that cannot be recorded (the legacy default stream) runs the
+    // sequence launch by launch
+    if (cudaStreamBeginCapture(rt_stream(), cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        on_ = false;
+        return;
+    }
     open_ = true;
     g_recording = true;
     count_ = 0;

@@ -123,3 +123,25 @@ def test_step_graphs_do_not_change_results(dtype, lanes, snapshots):
             assert np.array_equal(out[steps][k], out[0][k]), (steps, k)
     with pytest.raises(Exception):
         S.set_step_graphs(-1)
+
+
+def test_step_graphs_fall_back_on_the_legacy_default_stream():
+    """The legacy default stream cannot be recorded: a library stream set to it
+    runs simulate and backward launch by launch, with the same results."""
+    from sphadjoint_gb300 import _lib as LB
+    import ctypes as C
+    case = K.dambreak_case(theta_seed=4, jitter=0.05)
+    rng = np.random.default_rng(7)
+    case["cX"] = rng.standard_normal(case["X0"].shape)
+    case["cV"] = rng.standard_normal(case["X0"].shape)
+    L = S.load()
+    ref = run_gpu(case, 20, dtype="f64", seeds=linear_seeds(case), snapshots=3)
+    LB.check(L.sph_set_stream(C.c_void_p(1)))  # cudaStreamLegacy
+    try:
+        r0 = S.step_graph_counts()[0]
+        out = run_gpu(case, 20, dtype="f64", seeds=linear_seeds(case), snapshots=3)
+        assert S.step_graph_counts()[0] == r0
+    finally:
+        LB.check(L.sph_set_stream(None))
+    for k in ("X", "V", "gX", "gV", "gtheta"):
+        assert np.array_equal(out[k], ref[k]), k
