@@ -974,8 +974,9 @@ def main():
                     help="served: time-step range of the requests")
     ap.add_argument("--max-inflight", type=int, default=256,
                     help="served: most requests in flight in the packed server")
-    ap.add_argument("--hbm-budget-gb", type=float, default=160.0,
-                    help="served: admission budget")
+    ap.add_argument("--hbm-budget-gb", type=float, default=224.0,
+                    help="served: admission budget in GiB (of the GPU's 277; the rest holds "
+                         "the other workloads' buffers of the same run)")
     ap.add_argument("--instances", type=int, default=64, help="batched: number of instances")
     ap.add_argument("--model", default="reference", choices=sorted(MODELS),
                     help="physics: the reference's (linear EOS, Morris viscosity) or Tait + "
