@@ -29,7 +29,7 @@ SOURCES = {
     "sph_server.cu": [],
     "sph_design.cu": ["--fmad=false"],
 }
-DEPS = ["sph_common.cuh", "sph_kernels.cuh", "sph_coop.cuh", "sph_engine.cuh", "sph_pack.cuh",
+DEPS = ["sph_common.cuh", "sph_fixed.cuh", "sph_kernels.cuh", "sph_coop.cuh", "sph_engine.cuh", "sph_pack.cuh",
         "sph_iface.hpp"]
 
 

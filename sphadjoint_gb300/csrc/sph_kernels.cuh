@@ -18,6 +18,7 @@
 #pragma once
 
 #include "sph_common.cuh"
+#include "sph_fixed.cuh"
 
 namespace sphgb {
 
@@ -1347,58 +1348,16 @@ __device__ __forceinline__ void pass1_finish(const IT &I, int64_t i, const T2<T>
 
 // 128-bit two's-complement fixed-point accumulation: integer addition is
 // associative, so the dJ/dtheta sums are exact and independent of the order in
-// which particles arrive. acc[0] = low word, acc[1] = high word.
-__device__ __forceinline__ void fixed_add(unsigned long long *acc, double c, int S)
+// which particles arrive. acc[0] = low word, acc[1] = high word. Adds the grid
+// value of one contribution (sph_fixed.cuh) with 64-bit integer atomics and
+// an explicit carry.
+template <typename C>
+__device__ __forceinline__ void fixed_add(unsigned long long *acc, C c, int S)
 {
-    if (c == 0.0 || !isfinite(c)) return;
-    double a = rint(ldexp(fabs(c), S));
-    if (a == 0.0) return;
-    const double hid = floor(ldexp(a, -64));
-    const double lod = a - ldexp(hid, 64);
-    unsigned long long hi = (unsigned long long)hid;
-    unsigned long long lo = (unsigned long long)lod;
-    if (c < 0.0) {
-        lo = ~lo + 1ull;
-        hi = ~hi + (lo == 0ull ? 1ull : 0ull);
-    }
-    const unsigned long long old = atomicAdd(acc, lo);
-    const unsigned long long h = hi + ((old + lo < old) ? 1ull : 0ull);
-    if (h) atomicAdd(acc + 1, h);
-}
-
-// fixed_add of an FP32 contribution with integer instructions only: c is
-// M 2^E with a 24-bit integer M, so round(|c| 2^S) is M shifted by E + S,
-// rounded half to even when the shift drops bits, which is what the double
-// path's rint(ldexp(|c|, S)) gives for a float c (the double product is
-// exact). The same 128-bit integer reaches the accumulator without the
-// double-precision pipe, which runs at a small fraction of the FP32 rate.
-__device__ __forceinline__ void fixed_add(unsigned long long *acc, float c, int S)
-{
-    const uint32_t bits = __float_as_uint(c);
-    const uint32_t ex = (bits >> 23) & 0xffu;
-    if ((bits & 0x7fffffffu) == 0u || ex == 0xffu) return; // zero, inf, NaN
-    const uint32_t M = ex ? ((bits & 0x7fffffu) | 0x800000u) : (bits & 0x7fffffu);
-    const int k = (ex ? (int)ex - 150 : -149) + S;
-    if (k >= 104) { // beyond the 128-bit grid (cannot happen by the scale's bound)
-        fixed_add(acc, (double)c, S);
-        return;
-    }
-    unsigned __int128 v;
-    if (k >= 0) {
-        v = (unsigned __int128)M << k;
-    } else if (k <= -25) {
-        return; // below half a unit of the grid: rounds to 0
-    } else {
-        const int sh = -k;
-        const uint32_t q = M >> sh, r = M & ((1u << sh) - 1u), half = 1u << (sh - 1);
-        const uint32_t up = (r > half || (r == half && (q & 1u))) ? 1u : 0u;
-        v = (unsigned __int128)(q + up);
-    }
-    if (v == 0) return;
-    if (bits >> 31) v = ~v + 1;
-    const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
-    const unsigned long long old = atomicAdd(acc, lo);
-    const unsigned long long h = hi + ((old + lo < old) ? 1ull : 0ull);
+    Fixed128 v;
+    if (!fixed_of(c, S, v)) return;
+    const unsigned long long old = atomicAdd(acc, v.lo);
+    const unsigned long long h = v.hi + ((old + v.lo < old) ? 1ull : 0ull);
     if (h) atomicAdd(acc + 1, h);
 }
 
