@@ -56,6 +56,60 @@ template <typename T> __device__ __forceinline__ T r2_exact(T dx, T dy)
     return add_rn(mul_rn(dx, dx), mul_rn(dy, dy));
 }
 
+// Exact FP64 operations done on the bits with integer instructions: GB300
+// runs double-precision arithmetic at a small fraction of its integer rate,
+// and small FP64 states are bound by that pipe. Each gives the bits of the
+// FP64 instruction it replaces; the FP32 forms are the FP32 instructions.
+//
+// q / 2 (round to nearest even): the exponent minus one for a normal
+// result; a right shift of the significand, ties to even, for a subnormal or
+// zero one; inf and NaN unchanged.
+template <typename T> __device__ __forceinline__ T half_of(T q) { return (T)0.5 * q; }
+template <> __device__ __forceinline__ double half_of<double>(double q)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    unsigned long long r;
+    if (e >= 2u && e != 0x7ffu) {
+        r = b - (1ull << 52);
+    } else if (e == 0x7ffu) {
+        r = b;
+    } else {
+        const unsigned long long sign = b & (1ull << 63), m = b & ~(1ull << 63);
+        r = sign | ((m >> 1) + (m & (m >> 1) & 1ull));
+    }
+    return __longlong_as_double((long long)r);
+}
+
+// 2 q: the exponent plus one for a normal result; a left shift for a
+// subnormal or zero q (exact); infinity on overflow; inf and NaN unchanged.
+template <typename T> __device__ __forceinline__ T twice_of(T q) { return (T)2 * q; }
+template <> __device__ __forceinline__ double twice_of<double>(double q)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(q);
+    const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+    const unsigned long long sign = b & (1ull << 63);
+    unsigned long long r;
+    if (e != 0u && e < 0x7feu) r = b + (1ull << 52);
+    else if (e == 0u) r = sign | ((b & ~(1ull << 63)) << 1);
+    else if (e == 0x7feu) r = sign | 0x7ff0000000000000ull;
+    else r = b;
+    return __longlong_as_double((long long)r);
+}
+
+// a < b for a, b >= 0 and neither -0 (squared distances and their bounds):
+// non-negative doubles order like their bits as unsigned integers, and a NaN
+// compares false either way.
+template <typename T> __device__ __forceinline__ bool lt_nonneg(T a, T b) { return a < b; }
+template <> __device__ __forceinline__ bool lt_nonneg<double>(double a, double b)
+{
+    const unsigned long long ua = (unsigned long long)__double_as_longlong(a);
+    const unsigned long long ub = (unsigned long long)__double_as_longlong(b);
+    // a NaN has the largest exponent, so it is above every finite bound; a
+    // negative NaN's sign bit puts it above every non-negative bit pattern
+    return ua < ub && ub < 0x7ff0000000000001ull;
+}
+
 // Position of the r-th (0-based) set bit of m; requires r < popc(m).
 __device__ __forceinline__ int select_bit(uint32_t m, int r)
 {
@@ -228,7 +282,7 @@ __device__ __forceinline__ void for_each_neighbor(const NLView<T> &v, const Inst
             for (int j = b; j < e; ++j) {
                 const T2<T> xj = v.xref[j];
                 const T r2 = r2_exact<T>(sub_rn(xr.x, xj.x), sub_rn(xr.y, xj.y));
-                if (I.r2min < r2 && r2 < I.rc2) {
+                if (lt_nonneg(I.r2min, r2) && lt_nonneg(r2, I.rc2)) {
                     if (cnt < I.maxnb) {
                         ++cnt;
                         f(j);

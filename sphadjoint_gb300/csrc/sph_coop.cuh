@@ -144,7 +144,7 @@ __device__ __forceinline__ int spill_list(const Group<G> &g, const NLView<T> &v,
             if (j < e) {
                 const T2<T> xj = v.xref[j];
                 const T r2 = r2_exact<T>(sub_rn(xr.x, xj.x), sub_rn(xr.y, xj.y));
-                pass = I.r2min < r2 && r2 < I.rc2;
+                pass = lt_nonneg(I.r2min, r2) && lt_nonneg(r2, I.rc2);
             }
             uint32_t kept = g.ballot(pass);
             const int room = maxnb - cnt;
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                 if (j < e) {
                     const T2<T> xj = pos[j];
                     const T r2 = r2_exact<T>(sub_rn(xi.x, xj.x), sub_rn(xi.y, xj.y));
-                    pass = r2min < r2 && r2 < rc2;
+                    pass = lt_nonneg(r2min, r2) && lt_nonneg(r2, rc2);
                 }
                 uint32_t kept = g.ballot(pass);
                 const int np = __popc(kept), room = maxnb - m;
@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(kCoopBlock)
             const T dx = xi.x - xj.x;
             const T dy = xi.y - xj.y;
             const T r2 = dx * dx + dy * dy;
-            if (r2 < r2max) {
+            if (lt_nonneg(r2, r2max)) {
                 in = true;
                 c = density_pair<T>(r2, invh, m, A);
                 if (w >= 0) atomicOr(&tws[g.gi][w], 1u << bit);
@@ -325,7 +325,7 @@ __device__ __forceinline__ void accel_sum_coop(const Group<G> &g, T (*buf)[4][G]
             const T dx = xi.x - xj.x;
             const T dy = xi.y - xj.y;
             const T r2 = dx * dx + dy * dy;
-            if (r2 < r2max) {
+            if (lt_nonneg(r2, r2max)) {
                 in = true;
                 const T rhoj = vc.kind == 1 ? rho[j] : (T)0;
                 t = accel_pair<T>(r2, dx, dy, invh, m, Fc, vc, pti, iri, rhoi, rhoj, vi, prho[j],
@@ -482,7 +482,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                 const T dx = xi.x - xj.x;
                 const T dy = xi.y - xj.y;
                 const T r2 = dx * dx + dy * dy;
-                if (r2 < r2max) {
+                if (lt_nonneg(r2, r2max)) {
                     in = true;
                     const T rhoj = vc.kind == 1 ? rho[j] : (T)0;
                     t = pass1_pair<T>(r2, dx, dy, invh, m, Fc, Gc, vc, pti, iri, rhoi, rhoj, vi,
@@ -550,7 +550,7 @@ __global__ void __launch_bounds__(kCoopBlock)
             const T dx = xi.x - xj.x;
             const T dy = xi.y - xj.y;
             const T r2 = dx * dx + dy * dy;
-            if (r2 < r2max) {
+            if (lt_nonneg(r2, r2max)) {
                 const T w = pass2_weight<T>(r2, invh, m, Fc, gri, grho[j]);
                 gx += w * dx;
                 gy += w * dy;
@@ -571,7 +571,7 @@ __global__ void __launch_bounds__(kCoopBlock)
                 const T dx = xi.x - xj.x;
                 const T dy = xi.y - xj.y;
                 const T r2 = dx * dx + dy * dy;
-                if (r2 < r2max) {
+                if (lt_nonneg(r2, r2max)) {
                     in = true;
                     const T wt = pass2_weight<T>(r2, invh, m, Fc, gri, grho[j]);
                     tx = wt * dx;

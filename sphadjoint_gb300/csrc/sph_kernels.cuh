@@ -441,7 +441,7 @@ __device__ __forceinline__ void nl_build_one(int64_t N, const IT &I, int bi, int
         } else {
             r2 = r2_exact<T>(sub_rn(xi.x, xj.x), sub_rn(xi.y, xj.y));
         }
-        return (r2min < r2 && r2 < rc2) ? 1u : 0u;
+        return (lt_nonneg(r2min, r2) && lt_nonneg(r2, rc2)) ? 1u : 0u;
     };
     uint32_t lo[3], hi[3];
     int cnt[3]; // passing slots of each row, beyond 64 included
@@ -518,9 +518,9 @@ template <typename T>
 __device__ __forceinline__ T density_pair(T r2, T invh, T m, T A)
 {
     const T q = pair_sqrt(r2) * invh;
-    const T u = (T)1 - (T)0.5 * q;
+    const T u = (T)1 - half_of(q);
     const T u2 = u * u;
-    return m * (A * u2 * u2 * ((T)2 * q + (T)1));
+    return m * (A * u2 * u2 * (twice_of(q) + (T)1));
 }
 
 // Viscosity constants of one instance, hoisted out of the pair loops: kind 0
@@ -552,7 +552,7 @@ __device__ __forceinline__ AccelPair<T> accel_pair(T r2, T dx, T dy, T invh, T m
                                                    const T2<T> &vj)
 {
     const T q = pair_sqrt(r2) * invh;
-    const T u = (T)1 - (T)0.5 * q;
+    const T u = (T)1 - half_of(q);
     const T F = Fc * u * u * u;
     const T Pij = m * (pti + pj.x);
     AccelPair<T> o;
@@ -565,7 +565,7 @@ __device__ __forceinline__ AccelPair<T> accel_pair(T r2, T dx, T dy, T invh, T m
         T K = (T)0;
         if (s < (T)0) {
             const T D = r2 + vc.eh2;
-            const T rb = (rhoi + rhoj) * (T)0.5;
+            const T rb = half_of(rhoi + rhoj);
             K = vc.avc * s * F / (D * rb);
         }
         o.cx = K * dx;
@@ -604,7 +604,7 @@ __device__ __forceinline__ Pass1Pair<T> pass1_pair(T r2, T dx, T dy, T invh, T m
         r = sqrt(r2);
     }
     const T q = r * invh;
-    const T u = (T)1 - (T)0.5 * q;
+    const T u = (T)1 - half_of(q);
     const T F = Fc * u * u * u;
     const T G = Gc * u * u;
     const T Pij = m * (pti + pj.x);
@@ -629,19 +629,19 @@ __device__ __forceinline__ Pass1Pair<T> pass1_pair(T r2, T dx, T dy, T invh, T m
         T avx = (T)0, avy = (T)0, vx = (T)0, vy = (T)0, rs = (T)0;
         if (s < (T)0) {
             const T D = r2 + vc.eh2;
-            const T rb = (rhoi + rhoj) * (T)0.5;
+            const T rb = half_of(rhoi + rhoj);
             const T Drb = D * rb;
             const T K = vc.avc * s * F / Drb;
             const T Ks = vc.avc * F / Drb;
             const T KF = vc.avc * s / Drb;
             T cd;
-            if constexpr (sizeof(T) == 4) cd = Ad * (KF * G * invh * rinv - (T)2 * K / D);
-            else cd = Ad * (KF * G * invh / r - (T)2 * K / D);
+            if constexpr (sizeof(T) == 4) cd = Ad * (KF * G * invh * rinv - twice_of(K) / D);
+            else cd = Ad * (KF * G * invh / r - twice_of(K) / D);
             avx = K * dax + Ad * Ks * dvx + cd * dx;
             avy = K * day + Ad * Ks * dvy + cd * dy;
             vx = Ad * Ks * dx;
             vy = Ad * Ks * dy;
-            rs = Ad * K / ((T)2 * rb);
+            rs = Ad * K / twice_of(rb);
         }
         o.gxa = w * dx + avx;
         o.gya = w * dy + avy;
@@ -669,7 +669,7 @@ template <typename T>
 __device__ __forceinline__ T pass2_weight(T r2, T invh, T m, T Fc, T gri, T grj)
 {
     const T q = pair_sqrt(r2) * invh;
-    const T u = (T)1 - (T)0.5 * q;
+    const T u = (T)1 - half_of(q);
     return m * (Fc * u * u * u) * (gri + grj);
 }
 
@@ -687,7 +687,7 @@ __device__ __forceinline__ T density_spill_sum(const NLView<T> &v, const IT &I, 
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < r2max) acc += density_pair<T>(r2, invh, m, A);
+        if (lt_nonneg(r2, r2max)) acc += density_pair<T>(r2, invh, m, A);
     });
     if (tmaskOut)
         for (int w = 0; w < 6; ++w) tmaskOut[(int64_t)w * v.N + i] = 0u;
@@ -839,13 +839,13 @@ __device__ __forceinline__ void density_walk(const NLView<T> &v, int64_t i, T *_
                 // branch that diverges on the support test (13% faster on
                 // 1M particles); an outside candidate has u = 0 and adds 0.
                 // The common factor m A is applied once after the loop (8%).
-                const bool in = r2 < r2max;
+                const bool in = lt_nonneg(r2, r2max);
                 tw |= (uint32_t)in << k;
                 const T q = pair_sqrt(r2) * invh;
-                const T u = in ? (T)1 - (T)0.5 * q : (T)0;
+                const T u = in ? (T)1 - half_of(q) : (T)0;
                 const T u2 = u * u;
-                acc += u2 * u2 * ((T)2 * q + (T)1);
-            } else if (r2 < r2max) {
+                acc += u2 * u2 * (twice_of(q) + (T)1);
+            } else if (lt_nonneg(r2, r2max)) {
                 // FP64: the pipe is the bottleneck, so skip outside candidates
                 tw |= 1u << k;
                 acc += density_pair<T>(r2, invh, m, A);
@@ -942,12 +942,12 @@ __global__ void __launch_bounds__(32 * kTileWarps)
             const T dx = xi.x - xj.x;
             const T dy = xi.y - xj.y;
             const T r2 = dx * dx + dy * dy;
-            const bool in = listed && r2 < r2max;
+            const bool in = listed && lt_nonneg(r2, r2max);
             tw |= (uint64_t)in << (off & 63);
             const T q = pair_sqrt(r2) * invh;
-            const T u = in ? (T)1 - (T)0.5 * q : (T)0;
+            const T u = in ? (T)1 - half_of(q) : (T)0;
             const T u2 = u * u;
-            acc += u2 * u2 * ((T)2 * q + (T)1);
+            acc += u2 * u2 * (twice_of(q) + (T)1);
         }
         k0 += sn[r];
         if (tmaskOut) {
@@ -978,7 +978,7 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
         for_each_neighbor<T>(v, I, i, [&](int j) {
             const float2 d = fsub2(xi, v.pos[j]);
             const float r2 = d.x * d.x + d.y * d.y;
-            if (r2 < r2max) {
+            if (lt_nonneg(r2, r2max)) {
                 const float2 pj = prho[j];
                 const float q = pair_sqrt(r2) * invh;
                 const float u = 1.0f - 0.5f * q;
@@ -1001,7 +1001,7 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < r2max) {
+        if (lt_nonneg(r2, r2max)) {
             const T rhoj = (AV && vc.kind == 1) ? rho[j] : (T)0;
             const AccelPair<T> t = accel_pair<T, AV>(r2, dx, dy, invh, m, Fc, vc, pti, iri, rhoi,
                                                      rhoj, vi, prho[j], vel[j]);
@@ -1263,7 +1263,7 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
         for_each_neighbor<T>(v, I, i, [&](int j) {
             const float2 d = fsub2(xi, v.pos[j]);
             const float r2 = d.x * d.x + d.y * d.y;
-            if (r2 < r2max) {
+            if (lt_nonneg(r2, r2max)) {
                 const float2 pj = prho[j];
                 const float rinv = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
                 const float r = r2 * rinv;
@@ -1302,7 +1302,7 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < r2max) {
+        if (lt_nonneg(r2, r2max)) {
             const T rhoj = (AV && vc.kind == 1) ? rho[j] : (T)0;
             const Pass1Pair<T> t = pass1_pair<T, AV>(r2, dx, dy, invh, m, Fc, Gc, vc, pti, iri,
                                                      rhoi, rhoj, vi, ab, prho[j], abar[j], vel[j]);
@@ -1413,7 +1413,7 @@ __device__ __forceinline__ void pass2_sum(const NLView<T> &v, const IT &I, int64
         for_each_neighbor<T>(v, I, i, [&](int j) {
             const float2 d = fsub2(xi, v.pos[j]);
             const float r2 = d.x * d.x + d.y * d.y;
-            if (r2 < r2max) {
+            if (lt_nonneg(r2, r2max)) {
                 const float w = pass2_weight<float>(r2, invh, m, Fc, gri, grho[j]);
                 acc = ffma2(make_float2(w, w), d, acc);
             }
@@ -1429,7 +1429,7 @@ __device__ __forceinline__ void pass2_sum(const NLView<T> &v, const IT &I, int64
         const T dx = xi.x - xj.x;
         const T dy = xi.y - xj.y;
         const T r2 = dx * dx + dy * dy;
-        if (r2 < r2max) {
+        if (lt_nonneg(r2, r2max)) {
             const T w = pass2_weight<T>(r2, invh, m, Fc, gri, grho[j]);
             gx += w * dx;
             gy += w * dy;
