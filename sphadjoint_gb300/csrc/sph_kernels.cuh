@@ -976,17 +976,19 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
         const float tmm = vc.twomumass;
         float2 acc = make_float2(0.0f, 0.0f);
         for_each_neighbor<T>(v, I, i, [&](int j) {
-            const float2 d = fsub2(xi, v.pos[j]);
+            const float2 xj = v.pos[j];
+            const float2 pj = prho[j];
+            const float2 vj = vel[j];
+            const float2 d = fsub2(xi, xj);
             const float r2 = d.x * d.x + d.y * d.y;
             if (lt_nonneg(r2, r2max)) {
-                const float2 pj = prho[j];
                 const float q = pair_sqrt(r2) * invh;
                 const float u = 1.0f - 0.5f * q;
                 const float F = Fc * u * u * u;
                 const float PF = m * (pti + pj.x) * F;
                 const float C = tmm * iri * pj.y * F;
                 acc = ffma2(make_float2(-PF, -PF), d, acc);
-                acc = ffma2(make_float2(C, C), fsub2(vi, vel[j]), acc);
+                acc = ffma2(make_float2(C, C), fsub2(vi, vj), acc);
             }
         });
         ax = acc.x;
@@ -1261,10 +1263,13 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
         float2 g = make_float2(0.0f, 0.0f), gv = make_float2(0.0f, 0.0f);
         float gr = 0.0f, sS = 0.0f;
         for_each_neighbor<T>(v, I, i, [&](int j) {
-            const float2 d = fsub2(xi, v.pos[j]);
+            const float2 xj = v.pos[j];
+            const float2 pj = prho[j];
+            const float2 abj = abar[j];
+            const float2 vj = vel[j];
+            const float2 d = fsub2(xi, xj);
             const float r2 = d.x * d.x + d.y * d.y;
             if (lt_nonneg(r2, r2max)) {
-                const float2 pj = prho[j];
                 const float rinv = r2 > 0.0f ? rsqrtf(r2) : 0.0f;
                 const float r = r2 * rinv;
                 const float q = r * invh;
@@ -1274,8 +1279,8 @@ __device__ __forceinline__ void pass1_sum(const NLView<T> &v, const IT &I, int64
                 const float PF = m * (pti + pj.x) * F;
                 const float Cbase = tmm * iri * pj.y;
                 const float C = Cbase * F;
-                const float2 da = fsub2(ab, abar[j]);
-                const float2 dv = fsub2(vi, vel[j]);
+                const float2 da = fsub2(ab, abj);
+                const float2 dv = fsub2(vi, vj);
                 const float ad_d = -(da.x * d.x + da.y * d.y);
                 const float ad_v = da.x * dv.x + da.y * dv.y;
                 const float Fbar = m * (pti + pj.x) * ad_d + Cbase * ad_v;
@@ -1411,10 +1416,12 @@ __device__ __forceinline__ void pass2_sum(const NLView<T> &v, const IT &I, int64
     if constexpr (sizeof(T) == 4 && kPackedPairs) {
         float2 acc = make_float2(0.0f, 0.0f);
         for_each_neighbor<T>(v, I, i, [&](int j) {
-            const float2 d = fsub2(xi, v.pos[j]);
+            const float2 xj = v.pos[j];
+            const float grj = grho[j];
+            const float2 d = fsub2(xi, xj);
             const float r2 = d.x * d.x + d.y * d.y;
             if (lt_nonneg(r2, r2max)) {
-                const float w = pass2_weight<float>(r2, invh, m, Fc, gri, grho[j]);
+                const float w = pass2_weight<float>(r2, invh, m, Fc, gri, grj);
                 acc = ffma2(make_float2(w, w), d, acc);
             }
         });
