@@ -976,6 +976,9 @@ __device__ __forceinline__ void accel_sum(const NLView<T> &v, const Inst<T> &I,
         const float tmm = vc.twomumass;
         float2 acc = make_float2(0.0f, 0.0f);
         for_each_neighbor<T>(v, I, i, [&](int j) {
+            // all of the neighbour's loads before the support test: the
+            // in-support walk visits only pairs that pass it, and the later
+            // loads then do not wait for the position's latency
             const float2 xj = v.pos[j];
             const float2 pj = prho[j];
             const float2 vj = vel[j];
