@@ -122,7 +122,6 @@ void rt_after_launch(int kid)
 void rt_check_launch(const char *name) { cuda_check(cudaGetLastError(), name); }
 
 bool rt_capturing() { return g_capturing || g_recording; }
-bool rt_recording_steps() { return g_recording; }
 
 bool rt_timers_on()
 {
@@ -244,7 +243,6 @@ void StepGraphs::replay()
             (void)cudaGraphExecDestroy(hit->exec);
             hit->exec = nullptr;
             cuda_check(cudaGraphInstantiate(&hit->exec, g, 0), "cudaGraphInstantiate");
-            inst_ += 1;
             g_sg_inst.fetch_add(1, std::memory_order_relaxed);
         }
     } else {
@@ -257,14 +255,12 @@ void StepGraphs::replay()
         }
         cudaGraphExec_t x = nullptr;
         cuda_check(cudaGraphInstantiate(&x, g, 0), "cudaGraphInstantiate");
-        inst_ += 1;
         g_sg_inst.fetch_add(1, std::memory_order_relaxed);
         cache_.push_back({key, x, 0});
         hit = &cache_.back();
     }
     hit->used = ++clock_;
     cuda_check(cudaGraphLaunch(hit->exec, rt_stream()), "cudaGraphLaunch");
-    replays_ += 1;
     g_sg_replays.fetch_add(1, std::memory_order_relaxed);
 }
 

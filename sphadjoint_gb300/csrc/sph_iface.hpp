@@ -105,8 +105,6 @@ void rt_set_step_graph(int steps);
 // are skipped (results stay on the device) and device allocations are
 // refused.
 bool rt_capturing();
-// True while a group of steps is being recorded (not a caller's capture).
-bool rt_recording_steps();
 // True when any kernel timer is on (launches are then not grouped, so that
 // each one is timed on its own).
 bool rt_timers_on();
@@ -135,9 +133,6 @@ class StepGraphs {
     void finish();
     // error path: ends an open recording and drops it
     void abandon() noexcept;
-    // groups replayed and graphs instantiated so far
-    int64_t replays() const { return replays_; }
-    int64_t instantiations() const { return inst_; }
 
   private:
     void replay();
@@ -150,7 +145,6 @@ class StepGraphs {
     int per_ = 0, count_ = 0;
     bool on_ = false, open_ = false;
     uint64_t clock_ = 0;
-    int64_t replays_ = 0, inst_ = 0;
 };
 
 // Ends an open group of a StepGraphs when the scope is left by an exception.
