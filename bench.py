@@ -42,19 +42,27 @@ TUNE_STEPS = 32
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 1,048,576
 # particles, FP32 (the --set full captures summarised in profiles/*_1M_fp32.md)
 TRAFFIC_1M_F32 = {
-    "density": 38.241536e6 + 0.864512e6,
-    "accel_integrate": 55.135232e6 + 1.583616e6,
-    "accel_drag": 71.916288e6 + 4.792064e6,
-    "pass1": 76.107008e6 + 5.036544e6,
-    "pass2": 63.411712e6 + 0.571136e6,
+    "density": 38.243584e6 + 0.870144e6,
+    "accel_integrate": 55.135488e6 + 2.096640e6,
+    "accel_drag": 71.912192e6 + 3.559680e6,
+    "pass1": 76.111104e6 + 3.872512e6,
+    "pass2": 63.416832e6 + 0.484096e6,
 }
 
 # smsp__issue_active.avg.pct_of_peak_sustained_active of the same captures:
 # the fraction of cycles in which a warp scheduler issued, the bound these
 # gather kernels actually meet (HBM throughput stays in single digits)
 ISSUE_ACTIVE_1M_F32 = {
-    "density": 0.7646, "accel_integrate": 0.6868, "accel_drag": 0.6758,
-    "pass1": 0.6788, "pass2": 0.7340,
+    "density": 0.7623, "accel_integrate": 0.6856, "accel_drag": 0.6692,
+    "pass1": 0.7149, "pass2": 0.7357,
+}
+
+# lts__throughput.avg.pct_of_peak_sustained_elapsed and
+# l1tex__throughput.avg.pct_of_peak_sustained_active of the same captures:
+# neither cache level is near its peak either
+L2_L1_FRAC_1M_F32 = {
+    "density": (0.0803, 0.3387), "accel_integrate": (0.0900, 0.6129),
+    "accel_drag": (0.0929, 0.5730), "pass1": (0.0983, 0.6216), "pass2": (0.1094, 0.4152),
 }
 
 # algorithmic HBM bytes per particle per launch (compulsory traffic of the
@@ -761,6 +769,8 @@ def run_ours(args):
             "launches": kn.value,
             "issue_active_frac": (ISSUE_ACTIVE_1M_F32.get(args.kernel)
                                   if N == 1 << 20 and args.dtype == "f32" else None),
+            "l2_l1_throughput_frac": (L2_L1_FRAC_1M_F32.get(args.kernel)
+                                      if N == 1 << 20 and args.dtype == "f32" else None),
             "events": ("in the timed region" if args.kernel_events else
                        "second pass of the same K solves, events around each launch"),
             "events_pass": events_pass}
